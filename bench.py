@@ -1,0 +1,464 @@
+#!/usr/bin/env python
+"""Benchmark: Gterms/s of the shaded visibility DFT + direct-DFT reconstruction.
+
+One step = one vis-DFT pass (K visibilities x J pixels, geometric Moon
+occlusion inline) followed by one reconstruction pass over the same K x J
+terms: 2*K*J terms.  Workload: 10 MHz, 8 satellites on a 30 deg inclined
+300 km lunar orbit, 28 baselines x 65,536 snapshots = 1,835,008 float32 uvw,
+196,608 Fibonacci-sphere pixels (power-law diffuse sky + 500 point sources),
+synthetic and seeded.  Inputs (~40 MB) are smaller than L2, so L2 is flushed
+(a 256 MB write) before every timed step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU restatement (the FP64
+oracle, all host threads) on a bounded sample per step; where the reference's
+own CUDA kernels were built from its sources (oracle/_ref) it also times the
+reference's plain kernels (visscal + imagerecon of vissGen10M_shade) on the GPU.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gterms/s shaded vis-DFT + recon, 1 GB300, chosen vs plain at ≤1e-5 rel err"
+UNIT = "Gterms/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="cfg2_10MHz")
+    ap.add_argument("--precision", choices=["auto", "fast", "comp"], default="auto")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the baseline sample")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+def dist_setup():
+    import torch
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        torch.cuda.set_device(0)
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for r in csv.reader(f):
+                if len(r) >= 9:
+                    rows.append([x.strip() for x in r])
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((float(r[3]) for r in rows if r[3].replace(".", "").isdigit()), default=None)}
+
+
+# ------------------------------------------------------------------ workload
+def load_workload(name, device="cuda"):
+    import torch
+    from viss_recon_shade_gb300.synth import WORKLOADS, make_sky, make_uvw
+    wl = WORKLOADS[name]
+    d = make_uvw(wl, device=device)
+    l, m, n, b = make_sky(wl)
+    t = lambda a: torch.from_numpy(a).to(device)  # noqa: E731
+    d.update(l=t(l), m=t(m), n=t(n), b=t(b))
+    torch.cuda.synchronize()
+    return wl, d
+
+
+def choose_precision(d, pref):
+    import viss_recon_shade_gb300 as V
+    if pref == "fast":
+        return V.PREC_FAST
+    if pref == "comp":
+        return V.PREC_COMPENSATED
+    umax = max(float(d[k].abs().max()) for k in ("u", "v", "w"))
+    # the fast path's phase error grows as |uvw| * 2^-33 turns per coordinate
+    return V.PREC_FAST if umax <= 4096 else V.PREC_COMPENSATED
+
+
+def run_ours(args, ws, rank, local):
+    import torch
+    import viss_recon_shade_gb300 as V
+    from viss_recon_shade_gb300 import _lib as L
+    wl, d = load_workload(args.workload)
+    K, J = d["u"].numel(), d["l"].numel()
+    prec = choose_precision(d, args.precision)
+    cfg = V.DftConfig.north_star(precision=prec, occluded_value=0.0)
+    geo = dict(snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    Vout = torch.empty(K, dtype=torch.complex64, device="cuda")
+    Fout = torch.empty(J, dtype=torch.complex64, device="cuda")
+
+    def step():
+        V.vis_dft(cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
+        V.recon(cfg, d["u"], d["v"], d["w"], Vout, d["l"], d["m"], d["n"], out=Fout, **geo)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n0 = L.lib.viss_launch_count()
+    with ClockSampler(local) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0e.record(st)
+        for i in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps
+            ev[i][0].record(st)
+            V.vis_dft(cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
+            ev[i][1].record(st)
+            V.recon(cfg, d["u"], d["v"], d["w"], Vout, d["l"], d["m"], d["n"], out=Fout, **geo)
+            ev[i][2].record(st)
+        t1e.record(st)
+        torch.cuda.synchronize()
+        barrier(ws)
+    launches = int(L.lib.viss_launch_count() - n0)
+    total_ms = max_over_ranks(t0e.elapsed_time(t1e), ws)
+    vis_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    rec_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    terms_step = 2.0 * K * J
+    value = terms_step * args.steps * ws / (total_ms * 1e-3) / 1e9
+
+    # ---- e2e through the public API with host buffers ----------------------
+    host = {k: d[k].cpu().pin_memory() for k in ("u", "v", "w", "snap", "pair", "l", "m", "n", "b", "sat_pos")}
+    dev = {k: torch.empty_like(d[k]) for k in host}
+    hV = torch.empty(K, dtype=torch.complex64).pin_memory()
+    hF = torch.empty(J, dtype=torch.complex64).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = hV.numel() * 8 + hF.numel() * 8
+
+    def e2e_step():
+        for k in host:
+            dev[k].copy_(host[k], non_blocking=True)
+        g = dict(snap=dev["snap"], pair=dev["pair"], sat_pos=dev["sat_pos"])
+        Vd = V.vis_dft(cfg, dev["u"], dev["v"], dev["w"], dev["l"], dev["m"], dev["n"], dev["b"], **g)
+        Fd = V.recon(cfg, dev["u"], dev["v"], dev["w"], Vd, dev["l"], dev["m"], dev["n"], **g)
+        hV.copy_(Vd, non_blocking=True)
+        hF.copy_(Fd, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(2, min(args.steps, 5))
+    e0.record(st)
+    for _ in range(e2e_steps):
+        flush.zero_()
+        e2e_step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), ws)
+    e2e_value = terms_step * e2e_steps * ws / (e2e_ms * 1e-3) / 1e9
+
+    # ---- roofline: SFU pipe (2 SFU ops per term) ------------------------------
+    import ctypes as C
+    probe_out = torch.zeros(4, device="cuda")
+    ops = C.c_int64(0)
+    for _ in range(2):
+        L.check(L.lib.viss_sfu_probe(4096, 8, C.c_void_p(probe_out.data_ptr()), C.byref(ops),
+                                     C.c_void_p(st.cuda_stream)), "probe")
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pe0.record(st)
+    L.check(L.lib.viss_sfu_probe(4096, 8, C.c_void_p(probe_out.data_ptr()), C.byref(ops),
+                                 C.c_void_p(st.cuda_stream)), "probe")
+    pe1.record(st)
+    torch.cuda.synchronize()
+    sfu_peak = ops.value / (pe0.elapsed_time(pe1) * 1e-3) / 1e9  # G SFU ops / s
+    dom_ms, dom = (vis_ms, "vis_fast_kernel") if vis_ms >= rec_ms else (rec_ms, "recon_fast_kernel")
+    achieved = 2.0 * K * J / (dom_ms * 1e-3) / 1e9
+    props = torch.cuda.get_device_properties(0)
+    roofline = {"bound": "sfu", "kernel": dom, "achieved": round(achieved, 2), "peak": round(sfu_peak, 2),
+                "unit": "G SFU op/s", "frac": round(achieved / sfu_peak, 4),
+                "peak_source": "measured: viss_sfu_probe (8 independent __sincosf chains per thread) in this run",
+                "algorithmic_per_term": "2 SFU ops (sin, cos) + 6 FMA-pipe ops (vis) / 8 (recon)",
+                "traffic": None, "sm_count": props.multi_processor_count,
+                "vis_ms": round(vis_ms, 3), "recon_ms": round(rec_ms, 3)}
+
+    # ---- plain (the reference's FP32 method restated) -------------------------
+    plain = None
+    if not args.no_plain:
+        pcfg = cfg.with_(precision=V.PREC_PLAIN)
+        V.vis_dft(pcfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
+        torch.cuda.synchronize()
+        p0, p1, p2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        flush.zero_()
+        p0.record(st)
+        V.vis_dft(pcfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
+        p1.record(st)
+        V.recon(pcfg, d["u"], d["v"], d["w"], Vout, d["l"], d["m"], d["n"], out=Fout, **geo)
+        p2.record(st)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p2)
+        plain = {"value": round(terms_step / (pms * 1e-3) / 1e9, 3), "unit": UNIT,
+                 "vis_ms": round(p0.elapsed_time(p1), 2), "recon_ms": round(p1.elapsed_time(p2), 2),
+                 "what": "PREC_PLAIN: the reference's FP32 phase (u*l/d + ...), precise sincosf, "
+                         "one thread per visibility / pixel, same masks"}
+        step()  # restore the chosen outputs
+        torch.cuda.synchronize()
+
+    # ---- CPU baseline (oracle, bounded sample) + accuracy on the sample -------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, wl, d, Vout, Fout, cfg)
+
+    names = {V.PREC_FAST: "fast", V.PREC_COMPENSATED: "compensated"}
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fixed-point i32 phase)",
+            "data": "synthetic (seeded orbit + Fibonacci sky)",
+            "config": {"workload": wl.name, "K": K, "J": J, "terms_per_step": int(terms_step),
+                       "snapshots": wl.snapshots, "baselines": wl.npairs, "freq_hz": wl.freq_hz,
+                       "mask": "geometric", "precision": names.get(prec, str(prec)),
+                       "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
+            "plain": plain, "cpu_baseline": cpu}
+    if plain:
+        line["speedup_vs_plain"] = round(value / plain["value"], 2)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(args, wl, d, Vout, Fout, cfg):
+    """FP64 oracle (the reference formulas restated, OpenMP) on a bounded sample of
+    the workload: `nr` visibility rows x all pixels plus `np_` pixels x all
+    visibilities.  Also reports the GPU's error on exactly those rows/pixels."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    h = lambda t: t.cpu().numpy()  # noqa: E731
+    u, v, w, snap, pair, pos = (h(d[k]) for k in ("u", "v", "w", "snap", "pair", "sat_pos"))
+    l, m, n, b = (h(d[k]) for k in ("l", "m", "n", "b"))
+    K, J = u.size, l.size
+    thr = O.max_threads()
+    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=cfg.phase_scale, n_offset=cfg.n_offset,
+                      occluded_value=cfg.occluded_value, norm=1.0 / K)
+    # calibrate, then size the sample to ~cpu_seconds
+    rows = np.arange(0, K, max(1, K // 64))[:64]
+    t0 = time.perf_counter()
+    geo_s = O.make_geo(pos, snap[rows], pair[rows])
+    O.vis_dft(ocfg, u[rows], v[rows], w[rows], l, m, n, b, geo=geo_s, nthreads=thr)
+    rate = rows.size * J / (time.perf_counter() - t0)
+    target_terms = rate * args.cpu_seconds
+    nr = int(min(K, max(64, target_terms / 2 / J)))
+    np_ = int(min(J, max(16, target_terms / 2 / K)))
+    ridx = np.linspace(0, K - 1, nr).astype(np.int64)
+    pidx = np.linspace(0, J - 1, np_).astype(np.int64)
+    t0 = time.perf_counter()
+    geo_r = O.make_geo(pos, snap[ridx], pair[ridx])
+    Vo = O.vis_dft(ocfg, u[ridx], v[ridx], w[ridx], l, m, n, b, geo=geo_r, nthreads=thr)
+    geo_all = O.make_geo(pos, snap, pair)
+    Vg = h(Vout)
+    Fo = O.recon(ocfg, u, v, w, None, Vg, l[pidx], m[pidx], n[pidx], geo=geo_all, nthreads=thr)
+    dt = time.perf_counter() - t0
+    terms = nr * J + np_ * K
+    Fg = h(Fout)[pidx]
+    ev = np.linalg.norm(Vg[ridx] - Vo) / np.linalg.norm(Vo)
+    ef = np.linalg.norm(Fg - Fo) / np.linalg.norm(Fo)
+    evm = np.abs(Vg[ridx] - Vo).max() / np.abs(Vo).max()
+    efm = np.abs(Fg - Fo).max() / np.abs(Fo).max()
+    return {"value": round(terms / dt / 1e9, 4), "unit": UNIT, "cores": thr, "kind": "port",
+            "sample": f"FP64 oracle: {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities "
+                      f"({terms:.3g} terms, {dt:.1f} s)",
+            "gpu_rel_err_on_sample": {"vis_rms": float(ev), "vis_max": float(evm), "recon_rms": float(ef),
+                                      "recon_max": float(efm)}}
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, ws, rank, local):
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from oracle import oracle as O
+    O.build()
+    wl, d = load_workload(args.workload)
+    h = lambda t: t.cpu().numpy()  # noqa: E731
+    u, v, w, snap, pair, pos = (h(d[k]) for k in ("u", "v", "w", "snap", "pair", "sat_pos"))
+    l, m, n, b = (h(d[k]) for k in ("l", "m", "n", "b"))
+    K, J = u.size, l.size
+    thr = O.max_threads()
+    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=1.0, n_offset=-1.0, occluded_value=0.0, norm=1.0 / K)
+    geo_all = O.make_geo(pos, snap, pair)
+    # bounded sample per step: nr rows x J (vis) + np_ pixels x K (recon), ~3 s
+    rows = np.arange(0, K, max(1, K // 32))[:32]
+    t0 = time.perf_counter()
+    O.vis_dft(ocfg, u[rows], v[rows], w[rows], l, m, n, b, geo=O.make_geo(pos, snap[rows], pair[rows]), nthreads=thr)
+    rate = rows.size * J / (time.perf_counter() - t0)
+    tgt = rate * 3.0
+    nr = int(min(K, max(32, tgt / 2 / J)))
+    np_ = int(min(J, max(8, tgt / 2 / K)))
+    ridx = np.linspace(0, K - 1, nr).astype(np.int64)
+    pidx = np.linspace(0, J - 1, np_).astype(np.int64)
+    geo_r = O.make_geo(pos, snap[ridx], pair[ridx])
+    Vs = np.zeros(K, np.complex64)
+
+    def step():
+        Vo = O.vis_dft(ocfg, u[ridx], v[ridx], w[ridx], l, m, n, b, geo=geo_r, nthreads=thr)
+        Vs[ridx] = Vo
+        O.recon(ocfg, u, v, w, None, Vs, l[pidx], m[pidx], n[pidx], geo=geo_all, nthreads=thr)
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    terms = (nr * J + np_ * K) * args.steps
+    value = terms / dt / 1e9
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded orbit + Fibonacci sky)",
+            "impl": "reference",
+            "config": {"workload": wl.name, "K": K, "J": J, "mask": "geometric"},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": thr, "kind": "port",
+                             "sample": f"per step {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities, "
+                                       "FP64 restatement of visscal/imagerecon (oracle/viss_oracle.cpp)"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_ref_cuda:
+        line["ref_cuda_plain"] = ref_cuda_plain(wl, d)
+    print(json.dumps(line), flush=True)
+
+
+def ref_cuda_plain(wl, d):
+    """The reference's own plain kernels (vissGen10M_shade.cu visscal + imagerecon,
+    compiled from its sources into oracle/_ref) on the full workload, with its
+    REF window mask from the product's shade windows (RES 20940)."""
+    try:
+        import torch
+        from oracle import ref_cuda
+        import viss_recon_shade_gb300 as V
+        if not ref_cuda.available():
+            return {"unavailable": "reference kernels not built (oracle/_ref missing)"}
+        K, J = d["u"].numel(), d["l"].numel()
+        RES = 20940
+        raw, _ = V.shade_windows(d["u"], d["v"], d["w"], RES)
+        M = V.normalise_shade(raw)
+        Ms = [M[:, i].contiguous() for i in range(4)]
+        FF = d["b"]
+        nxq = torch.arange(J, dtype=torch.float32, device="cuda")
+        cl = torch.ones(J, dtype=torch.int32, device="cuda")
+        wgt = torch.ones(K, dtype=torch.float32, device="cuda")
+        nclip = d["n"].clamp(-1, 1)
+        args = (d["u"], d["v"], d["w"], d["l"], d["m"], nclip)
+        st = torch.cuda.current_stream()
+        ref_cuda.visscal("vissGen10M_shade", 8192, J, RES, FF, *args, *[x[:8192] for x in Ms], nxq, cl)
+        torch.cuda.synchronize()
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(st)
+        viss = ref_cuda.visscal("vissGen10M_shade", K, J, RES, FF, *args, *Ms, nxq, cl)
+        e1.record(st)
+        ref_cuda.imagerecon("vissGen10M_shade", K, J, RES, viss, *args, wgt, *Ms)
+        e2.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e2)
+        return {"value": round(2.0 * K * J / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
+                "vis_ms": round(e0.elapsed_time(e1), 1), "recon_ms": round(e1.elapsed_time(e2), 1),
+                "what": "reference vissGen10M_shade visscal + imagerecon, unmodified device code, "
+                        "REF window mask, one pass"}
+    except Exception as e:  # reported, not fatal: the CPU line above is the reference arm
+        return {"unavailable": f"{type(e).__name__}: {e}"}
+
+
+def main():
+    args = parse_args()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * viss_gb300.h -- C ABI of libvissgb.so, the GB300-native (sm_103a) hot path of
+ * the SSshuishui/viss_recon_shade lunar-orbit interferometry simulator:
+ *
+ *   orbit positions + baseline uvw   (MIncline_generate_uvw_float.cu:83-160, 350-397)
+ *   Moon shade windows               (shade1M.cu:62-105, 218-225)
+ *   shaded visibility DFT            (visscal, vissGen10M_shade.cu:108-145)
+ *   direct-DFT reconstruction        (imagerecon, vissGen10M_shade.cu:149-175)
+ *
+ * Conventions
+ *   - Every entry point returns VISS_OK (0) or a negative status; it never
+ *     exits the process.  viss_last_error() gives a message for the calling
+ *     thread's last failure.
+ *   - All array arguments are DEVICE pointers owned by the caller, unless a
+ *     comment says "host".  Complex values are interleaved float pairs
+ *     (re, im), i.e. the layout of thrust::complex<float> / complex64.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     Work is enqueued on it; calls return without synchronising unless noted.
+ *   - Scratch memory comes from a caller workspace whose size the matching
+ *     *_workspace() query returns (256-byte aligned).  The reference-shaped
+ *     entry points viss_visscal / viss_imagerecon allocate their workspace
+ *     stream-ordered (cudaMallocAsync) instead.
+ *   - Thread-safe: no global mutable state besides the thread-local error text.
+ */
+#ifndef VISS_GB300_H
+#define VISS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define VISS_API __attribute__((visibility("default")))
+#else
+#define VISS_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  VISS_OK = 0,
+  VISS_ERR_INVALID = -1,     /* null pointer, negative size, unknown mode */
+  VISS_ERR_WORKSPACE = -2,   /* workspace missing, too small or misaligned */
+  VISS_ERR_CUDA = -3,        /* a CUDA runtime call failed */
+  VISS_ERR_RANGE = -4,       /* input outside the supported range */
+  VISS_ERR_TIMEOUT = -5,     /* a bounded device-side wait gave up */
+  VISS_ERR_UNSUPPORTED = -6, /* combination not implemented */
+  VISS_ERR_IO = -7,          /* file could not be opened / written */
+  VISS_ERR_FORMAT = -8       /* file content does not parse */
+};
+
+/* Replaces the reference's CHECK() macro (error.cuh:3-18), which exits. */
+VISS_API const char* viss_status_str(int status);
+VISS_API const char* viss_last_error(void);
+VISS_API int viss_version(void);
+/* Number of kernels the calling thread's viss_* calls have launched so far
+ * (library-internal CUB kernels of viss_dedup_uvw not included). */
+VISS_API uint64_t viss_launch_count(void);
+
+/* ------------------------------------------------------------------ modes */
+enum {                         /* which (visibility, pixel) terms are occluded */
+  VISS_MASK_NONE = 0,
+  VISS_MASK_REF_QUIRK = 1,     /* vissGen10M_shade.cu:130 as written: window rows run only
+                                  when M3 <= 0, then rows 0..M4; cols M1 < c < M2           */
+  VISS_MASK_REF_INTENDED = 2,  /* rows M3..M4, cols M1 < c < M2                              */
+  VISS_MASK_GEOMETRIC = 3      /* ray from either satellite of the baseline hits the Moon   */
+};
+enum {                         /* recon-side mask */
+  VISS_RECON_MASK_NONE = 0,
+  VISS_RECON_MASK_REF = 1,     /* |M1/M2-thetaP|<M1/M2 && |M3/M4-phiP|<M3/M4 (vissGen10M_shade.cu:166) */
+  VISS_RECON_MASK_GEOMETRIC = 2
+};
+enum {                         /* phase + sincos arithmetic */
+  VISS_PREC_PLAIN = 0,         /* the reference's FP32 formula, precise sinf/cosf, 1 thread per item */
+  VISS_PREC_FAST = 1,          /* 32-bit fixed-point phase (exact mod 1 for integer uvw), SFU sincos */
+  VISS_PREC_COMPENSATED = 2    /* FAST + FP32 correction of the pixel fixed-point rounding */
+};
+
+/* One DFT pass.  Phase in turns: t = phase_scale * (u l + v m + w (n + n_offset)).
+ * vis:   V_k = sum_j C_kj exp(-2 pi i t_kj),  C_kj = occluded_value inside the mask else bright_j
+ * recon: F_j = norm * sum_k [not masked] wgt_k V_k exp(+2 pi i t_kj)
+ * The reference uses phase_scale = 1/d with d = 2*RES/(RES-1) in integer arithmetic (= 2),
+ * n_offset = 0 (its w(n-1) term and trailing e^{-2 pi i w/d} combine to w n), occluded_value 240,
+ * norm = 1/K.  The spec convention is phase_scale = 1, n_offset = -1, occluded_value 0. */
+typedef struct viss_dft_cfg {
+  int32_t mask_mode;         /* VISS_MASK_* (vis) */
+  int32_t recon_mask;        /* VISS_RECON_MASK_* (recon) */
+  int32_t precision;         /* VISS_PREC_* */
+  int32_t res;               /* fine-grid row width for the REF masks */
+  int32_t trunc_brightness;  /* 1: brightness truncated to int first (plain visscal, :128) */
+  float occluded_value;      /* brightness inside the vis mask */
+  double phase_scale;
+  double n_offset;
+  double moon_radius_km;     /* GEOMETRIC */
+  double norm;               /* recon output scale */
+} viss_dft_cfg;
+
+typedef struct viss_sky {    /* J sky pixels: direction cosines and brightness */
+  const float* l;
+  const float* m;
+  const float* n;
+  const float* bright;       /* vis only; may be NULL for recon */
+  int64_t J;
+} viss_sky;
+
+typedef struct viss_vis_set { /* K visibilities */
+  const float* u;            /* in wavelengths */
+  const float* v;
+  const float* w;
+  const float* wgt;          /* recon weight per visibility (reference: 1/freq or 1/count); NULL = 1 */
+  const int32_t* shade;      /* K x 4 normalised windows (M1<=M2, M3<=M4, 0-based); REF masks */
+  const int32_t* snap;       /* K snapshot index; GEOMETRIC */
+  const int32_t* pair;       /* K satellite pair, m | (n << 16); GEOMETRIC */
+  int64_t K;
+} viss_vis_set;
+
+typedef struct viss_geometry { /* satellite positions per snapshot; GEOMETRIC */
+  const float* sat_pos;      /* S x nsat x 3, km, Moon-centred */
+  int64_t S;
+  int32_t nsat;
+  int32_t reserved;
+} viss_geometry;
+
+/* Shaded visibility DFT (replaces visscal, vissGen10M_shade.cu:108-145 and its
+ * launchers, vissGen10M_shade_optim2.cu:150-215).  V: K x 2 float. */
+VISS_API size_t viss_vis_dft_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo);
+VISS_API int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                 const viss_geometry* geo, float* V, void* workspace, size_t workspace_bytes,
+                 void* stream);
+
+/* Direct-DFT reconstruction (replaces imagerecon, vissGen10M_shade.cu:149-175,
+ * and launch_imagerecon, vissGen10M_shade_optim2.cu:320-389).  V: K x 2, F: J x 2.
+ * With norm = 1, wgt = NULL and the vis mask this is the adjoint of viss_vis_dft
+ * with respect to the brightness. */
+VISS_API size_t viss_recon_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo);
+VISS_API int viss_recon(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+               const viss_geometry* geo, const float* V, float* F, void* workspace,
+               size_t workspace_bytes, void* stream);
+
+/* Reference-shaped operators: the argument lists of the reference kernels
+ * (the complex constants I1, CPI, zero, two are implied).  variant selects the
+ * brightness arithmetic: VISS_VARIANT_PLAIN truncates FF to int (vissGen10M_shade.cu:128),
+ * VISS_VARIANT_OPTIM keeps it float (vissGen10M_shade_optim1.cu:180).
+ * NXq/countLoc may both be NULL for the identity fine->coarse map (countLoc = 1,
+ * NXq[j] = j); otherwise NXq holds float indices as in the 10M files.
+ * mask_mode is VISS_MASK_REF_QUIRK for the reference's behaviour. */
+enum { VISS_VARIANT_PLAIN = 0, VISS_VARIANT_OPTIM = 1 };
+VISS_API int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float* viss,
+                 const float* u, const float* v, const float* w, const float* l, const float* m,
+                 const float* n, const int* shadeM1, const int* shadeM2, const int* shadeM3,
+                 const int* shadeM4, const float* NXq, const int* countLoc, float dl, float dm,
+                 float dn, int variant, int mask_mode, int precision, void* stream);
+VISS_API int viss_imagerecon(int uvw_index, int lmnC_index, int res, float* F, const float* viss,
+                    const float* u, const float* v, const float* w, const float* l, const float* m,
+                    const float* n, const float* uvwFrequencyMap, const float* thetaP0,
+                    const float* phiP0, const float* dtheta, const float* dphi, float dl, float dm,
+                    float dn, int precision, void* stream);
+
+/* ---------------------------------------------------------- orbit + uvw */
+typedef struct viss_orbit_cfg {  /* MIncline_generate_uvw_float.cu:22-30, 184-190 */
+  int32_t nsat;
+  int32_t orbit_res;      /* samples per orbit (reference 864000 = 2.4*3600/0.01) */
+  int32_t orbit_counts;   /* orbits (reference 140) */
+  int32_t index;          /* observation period, >= 1 */
+  double a_km;            /* orbit radius (reference 2038.14) */
+  double e;               /* eccentricity (reference 0) */
+  double incl_deg;        /* reference 30 */
+  double argp_deg;        /* reference 0 */
+  double raan_step_deg;   /* node advance per orbit (reference 0.08) */
+  const float* r1_m;      /* HOST [nsat] separation ramp ends (reference r1) */
+  const float* r2_m;      /* HOST [nsat] separation ramp middle (reference r2) */
+  int32_t fp64;           /* 0: reference FP32 arithmetic; 1: FP64 positions */
+  int32_t reserved;
+} viss_orbit_cfg;
+
+/* Number of windowed snapshots: orbit_counts * (orbit_res / 3). */
+VISS_API int64_t viss_orbit_snapshots(const viss_orbit_cfg* cfg);
+/* Satellite positions at every snapshot (calculateOrbit + uvwPosition, :83-151):
+ * pos: S x nsat x 3 float (km); pos64 (optional, may be NULL): the same in double. */
+VISS_API int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, void* stream);
+/* Baseline uvw (computeUVW, :153-160), snapshot-major then pair.  pairs: 1 = ordered
+ * (m != n, the reference's 56 for 8 satellites), 0 = unordered (m < n).  rounding: 1 = the
+ * reference's ceil(), 0 = none.  From pos64 when given (no rounding to float first).
+ * snap/pair outputs may be NULL.  K = S * npairs entries are written. */
+VISS_API int viss_baseline_uvw(const float* pos, const double* pos64, int64_t S, int32_t nsat, int ordered,
+                      double lambda_m, int rounding, float* u, float* v, float* w, int32_t* snap,
+                      int32_t* pair, void* stream);
+/* Global lexicographic sort + unique of integer-valued uvw (the reference's per-pair and
+ * global thrust sort/unique, :370-397).  In place on u, v, w; *count_out (HOST) receives
+ * the unique count (the call synchronises the stream).  |u|,|v|,|w| must be < 2^20. */
+VISS_API size_t viss_dedup_uvw_workspace(int64_t K);
+VISS_API int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------- shade windows */
+/* Cart2SphKernel + mean radius + ShadeMatrix (shade1M.cu:62-105, 218-225).
+ * out: K x 4 int32 (thetaIndS, thetaIndE, phiIndS, phiIndE), 1-based as in the shadeM files.
+ * mean_r_km > 0 uses that mean radius; otherwise it is computed (double sum) and, if
+ * mean_r_out (HOST) is non-NULL, returned there (the call then synchronises the stream). */
+VISS_API size_t viss_shade_windows_workspace(int64_t K);
+VISS_API int viss_shade_windows(const float* u, const float* v, const float* w, int64_t K, int RES,
+                       double mean_r_km, int32_t* out, double* mean_r_out, void* workspace,
+                       size_t workspace_bytes, void* stream);
+/* shadeM normalisation on load (vissGen10M_shade.cu:383-399): (min-1, max-1) per pair. */
+VISS_API int viss_normalise_shade(const int32_t* raw, int64_t K, int32_t* M, void* stream);
+
+/* ------------------------------------------------------------- measurement */
+/* SFU throughput probe (no counterpart in the reference): launches
+ * blocks_per_sm * SMs blocks of 256 threads, each thread running `iters` rounds of
+ * 8 independent __sincosf; *sfu_ops (HOST) receives the number of SFU operations
+ * (2 per sincos).  The caller times the launch on `stream`. */
+VISS_API int viss_sfu_probe(int iters, int blocks_per_sm, float* out, int64_t* sfu_ops, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VISS_GB300_H */

@@ -1,0 +1,66 @@
+"""The C ABI library: loads, exports every declared entry point, and rejects bad
+arguments with status codes before touching a GPU."""
+import ctypes as C
+
+import pytest
+
+
+@pytest.fixture(scope="module")
+def L():
+    from viss_recon_shade_gb300 import _lib
+    return _lib
+
+
+def test_exports_every_declared_symbol(L):
+    declared = L.declared_symbols()
+    assert len(declared) >= 18
+    for name in declared:
+        assert hasattr(L.lib, name), name
+    import subprocess
+    out = subprocess.run(["nm", "-D", "--defined-only", str(L.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    assert set(declared) <= exported
+
+
+def test_status_strings(L):
+    for s in (0, -1, -2, -3, -4, -5, -6, -7, -8):
+        assert L.lib.viss_status_str(s)
+    assert L.lib.viss_status_str(0) == b"ok"
+    assert L.lib.viss_version() >= 10000
+
+
+def test_invalid_arguments_fail_without_gpu(L):
+    # NULL config, bad modes and bad sizes are rejected on the host
+    assert L.lib.viss_vis_dft(None, None, None, None, None, None, 0, None) == L.VISS_ERR_INVALID
+    cfg = L.DftCfg(9, 0, 1, 0, 0, 0.0, 0.5, 0.0, 1737.4, 1.0)
+    sky = L.Sky(None, None, None, None, 0)
+    vis = L.VisSet(None, None, None, None, None, None, None, 0)
+    assert L.lib.viss_vis_dft(C.byref(cfg), C.byref(sky), C.byref(vis), None, None, None, 0, None) == \
+        L.VISS_ERR_INVALID
+    cfg.mask_mode = 0
+    cfg.phase_scale = 2.0
+    assert L.lib.viss_vis_dft(C.byref(cfg), C.byref(sky), C.byref(vis), None, None, None, 0, None) == L.VISS_ERR_RANGE
+    assert b"phase_scale" in L.lib.viss_last_error()
+    cfg.phase_scale = 0.5
+    cfg.mask_mode = 3  # geometric without geometry
+    vis.K = 5
+    sky.J = 3
+    dummy = C.c_void_p(16)
+    vis.u = vis.v = vis.w = dummy
+    sky.l = sky.m = sky.n = sky.bright = dummy
+    assert L.lib.viss_vis_dft(C.byref(cfg), C.byref(sky), C.byref(vis), None, dummy, None, 0, None) == \
+        L.VISS_ERR_INVALID
+    assert L.lib.viss_visscal(-1, 3, 10, *([None] * 14), 2.0, 2.0, 2.0, 0, 1, 1, None) == L.VISS_ERR_RANGE
+    assert L.lib.viss_dedup_uvw(None, None, None, 5, None, None, 0, None) == L.VISS_ERR_INVALID
+    oc = L.OrbitCfg(1, 360, 1, 1, 2038.14, 0.0, 30.0, 0.0, 0.08, None, None, 0, 0)
+    assert L.lib.viss_orbit_positions(C.byref(oc), dummy, None, None) == L.VISS_ERR_RANGE
+
+
+def test_workspace_queries_are_consistent(L):
+    cfg = L.DftCfg(3, 2, 1, 0, 0, 0.0, 1.0, -1.0, 1737.4, 1.0)
+    geo = L.Geometry(None, 100, 8, 0)
+    a = L.lib.viss_vis_dft_workspace(C.byref(cfg), 10000, 5000, C.byref(geo))
+    b = L.lib.viss_recon_workspace(C.byref(cfg), 10000, 5000, C.byref(geo))
+    assert a > 0 and b > 0 and a % 256 == 0 and b % 256 == 0
+    cfg.precision = 0  # plain needs no records
+    assert L.lib.viss_vis_dft_workspace(C.byref(cfg), 10000, 5000, C.byref(geo)) < a

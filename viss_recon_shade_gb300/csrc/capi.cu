@@ -1,0 +1,520 @@
+// capi.cu -- the extern "C" entry points of libvissgb.so for the DFT passes:
+// argument checks, workspace layout, launch planning and kernel dispatch.
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+
+#include "viss_internal.cuh"
+
+namespace viss {
+
+thread_local std::string g_last_error;
+thread_local uint64_t g_launches = 0;
+
+void count_launch() { ++g_launches; }
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+int fail(int status, const std::string& msg) {
+  g_last_error = msg;
+  return status;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return VISS_ERR_CUDA;
+}
+
+int device_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 148;
+  return n;
+}
+
+int launch_prep_recon_ratios(const float* thetaP0, const float* phiP0, const float* dtheta, const float* dphi,
+                             int64_t K, int64_t Kpad, int4* win, int* flags, cudaStream_t st);
+
+static inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+// ------------------------------------------------------------------ plans
+// Layout of the workspace of one vis pass.  Chosen from (K, J, mode) only, so
+// the size query and the call agree.
+struct VisPlan {
+  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, nrb = 0, jchunk = 0, nsd = 0;
+  int nsplit = 1;
+  bool geo = false, ref = false, comp = false, plain = false;
+  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *rows1 = nullptr, *win = nullptr;
+  float4 *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *cones = nullptr;
+  int2* pqr = nullptr;
+  float2* partial = nullptr;
+  int* flags = nullptr;
+  size_t bytes = 0;
+
+  void layout(void* ws) {
+    Carver c(ws);
+    flags = c.take<int>(64);
+    if (!plain) {
+      pix0 = c.take<int4>(Jpad);
+      pix1 = c.take<int4>(Jpad);
+      if (comp) plo = c.take<float4>(Jpad);
+      if (geo) pgeo = c.take<float4>(Jpad);
+      if (ref) pqr = c.take<int2>(Jpad);
+      rows0 = c.take<int4>(Kpad);
+      rows1 = c.take<int4>(Kpad);
+      if (comp) rowsf = c.take<float4>(Kpad);
+      if (ref) win = c.take<int4>(Kpad);
+      if (geo) { satdir = c.take<float4>(nsd); cones = c.take<float4>(2 * nrb); }
+      if (nsplit > 1) partial = c.take<float2>((size_t)nsplit * K);
+    }
+    bytes = c.size();
+  }
+};
+
+static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, const viss_geometry* geo) {
+  p.K = K; p.J = J;
+  p.plain = cfg.precision == VISS_PREC_PLAIN;
+  p.geo = cfg.mask_mode == VISS_MASK_GEOMETRIC;
+  p.ref = cfg.mask_mode == VISS_MASK_REF_QUIRK || cfg.mask_mode == VISS_MASK_REF_INTENDED;
+  p.comp = cfg.precision == VISS_PREC_COMPENSATED;
+  p.Jpad = round_up(J > 0 ? J : 1, REC_PIX);
+  p.Kpad = round_up(K > 0 ? K : 1, VIS_ROWS);
+  p.nrb = p.Kpad / VIS_ROWS;
+  p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
+  // Split the pixel axis when the visibility blocks alone fill less than
+  // ~4 waves of resident CTAs (3 per SM at 256 threads).
+  const int64_t slots = (int64_t)device_sm_count() * 3;
+  int64_t nsplit = 1;
+  if (p.nrb < 4 * slots) nsplit = (4 * slots + p.nrb - 1) / p.nrb;
+  const int64_t maxsplit = (J + VIS_P - 1) / VIS_P;
+  if (nsplit > maxsplit) nsplit = maxsplit;
+  if (nsplit < 1) nsplit = 1;
+  p.jchunk = round_up((J + nsplit - 1) / nsplit, VIS_P);
+  if (p.jchunk <= 0) p.jchunk = VIS_P;
+  p.nsplit = (int)((J + p.jchunk - 1) / p.jchunk);
+  if (p.nsplit < 1) p.nsplit = 1;
+  p.layout(nullptr);
+}
+
+struct RecPlan {
+  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, npb = 0, kchunk = 0, nsd = 0, S = 0;
+  int nsplit = 1;
+  bool geo = false, ref = false, comp = false, plain = false;
+  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *rows1 = nullptr, *win = nullptr;
+  float4 *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *scones = nullptr;
+  int2* pqr = nullptr;
+  float2 *y = nullptr, *partial = nullptr;
+  float* ratios = nullptr;
+  int* flags = nullptr;
+  size_t bytes = 0;
+
+  void layout(void* ws) {
+    Carver c(ws);
+    flags = c.take<int>(64);
+    if (plain) {
+      if (ref) ratios = c.take<float>(2 * (size_t)Kpad);
+    } else {
+      pix0 = c.take<int4>(Jpad);
+      pix1 = c.take<int4>(Jpad);
+      if (comp) plo = c.take<float4>(Jpad);
+      if (geo) pgeo = c.take<float4>(Jpad);
+      if (ref) pqr = c.take<int2>(Jpad);
+      rows0 = c.take<int4>(Kpad);
+      rows1 = c.take<int4>(Kpad);
+      if (comp) rowsf = c.take<float4>(Kpad);
+      if (ref) win = c.take<int4>(Kpad);
+      y = c.take<float2>(Kpad);
+      if (geo) { satdir = c.take<float4>(nsd); scones = c.take<float4>(2 * S); }
+      if (nsplit > 1) partial = c.take<float2>((size_t)nsplit * J);
+    }
+    bytes = c.size();
+  }
+};
+
+static void plan_recon(RecPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, const viss_geometry* geo) {
+  p.K = K; p.J = J;
+  p.plain = cfg.precision == VISS_PREC_PLAIN;
+  p.geo = cfg.recon_mask == VISS_RECON_MASK_GEOMETRIC;
+  p.ref = cfg.recon_mask == VISS_RECON_MASK_REF;
+  p.comp = cfg.precision == VISS_PREC_COMPENSATED;
+  p.Jpad = round_up(J > 0 ? J : 1, REC_PIX);
+  p.Kpad = round_up(K > 0 ? K : 1, VIS_ROWS);
+  p.npb = p.Jpad / REC_PIX;
+  p.S = (geo && p.geo) ? geo->S : 0;
+  p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
+  const int64_t slots = (int64_t)device_sm_count() * 2;
+  int64_t nsplit = 1;
+  if (p.npb < 4 * slots) nsplit = (4 * slots + p.npb - 1) / p.npb;
+  const int64_t maxsplit = (K + REC_Q - 1) / REC_Q;
+  if (nsplit > maxsplit) nsplit = maxsplit;
+  if (nsplit < 1) nsplit = 1;
+  p.kchunk = round_up((K + nsplit - 1) / nsplit, REC_Q);
+  if (p.kchunk <= 0) p.kchunk = REC_Q;
+  p.nsplit = (int)((K + p.kchunk - 1) / p.kchunk);
+  if (p.nsplit < 1) p.nsplit = 1;
+  p.layout(nullptr);
+}
+
+// ------------------------------------------------------------------ checks
+static int check_cfg(const viss_dft_cfg* cfg) {
+  if (!cfg) return fail(VISS_ERR_INVALID, "cfg is NULL");
+  if (cfg->mask_mode < VISS_MASK_NONE || cfg->mask_mode > VISS_MASK_GEOMETRIC)
+    return fail(VISS_ERR_INVALID, "mask_mode out of range");
+  if (cfg->recon_mask < VISS_RECON_MASK_NONE || cfg->recon_mask > VISS_RECON_MASK_GEOMETRIC)
+    return fail(VISS_ERR_INVALID, "recon_mask out of range");
+  if (cfg->precision < VISS_PREC_PLAIN || cfg->precision > VISS_PREC_COMPENSATED)
+    return fail(VISS_ERR_INVALID, "precision out of range");
+  if (!(cfg->phase_scale > 0.0) || !(cfg->phase_scale <= 1.0))
+    return fail(VISS_ERR_RANGE, "phase_scale must be in (0, 1]");
+  if (!(cfg->n_offset >= -1.0 && cfg->n_offset <= 0.0)) return fail(VISS_ERR_RANGE, "n_offset must be in [-1, 0]");
+  return VISS_OK;
+}
+
+static int check_geo(const viss_geometry* geo, const viss_vis_set* vis, const viss_dft_cfg* cfg) {
+  if (!geo || !geo->sat_pos) return fail(VISS_ERR_INVALID, "GEOMETRIC mask needs satellite positions");
+  if (geo->nsat < 1 || geo->nsat > 32) return fail(VISS_ERR_RANGE, "nsat must be in [1, 32]");
+  if (geo->S < 1) return fail(VISS_ERR_INVALID, "geometry has no snapshots");
+  if (!vis->snap || !vis->pair) return fail(VISS_ERR_INVALID, "GEOMETRIC mask needs snap and pair per visibility");
+  if (!(cfg->moon_radius_km > 0.0)) return fail(VISS_ERR_RANGE, "moon_radius_km must be > 0");
+  return VISS_OK;
+}
+
+static int check_sky(const viss_sky* sky, bool need_bright) {
+  if (!sky) return fail(VISS_ERR_INVALID, "sky is NULL");
+  if (sky->J < 0 || sky->J > (int64_t)1 << 30) return fail(VISS_ERR_RANGE, "J out of range");
+  if (sky->J > 0 && (!sky->l || !sky->m || !sky->n)) return fail(VISS_ERR_INVALID, "sky l/m/n NULL");
+  if (need_bright && sky->J > 0 && !sky->bright) return fail(VISS_ERR_INVALID, "sky brightness NULL");
+  return VISS_OK;
+}
+
+static int check_vis(const viss_vis_set* vis) {
+  if (!vis) return fail(VISS_ERR_INVALID, "vis set is NULL");
+  if (vis->K < 0 || vis->K > (int64_t)1 << 31) return fail(VISS_ERR_RANGE, "K out of range");
+  if (vis->K > 0 && (!vis->u || !vis->v || !vis->w)) return fail(VISS_ERR_INVALID, "u/v/w NULL");
+  return VISS_OK;
+}
+
+static int check_ws(void* ws, size_t have, size_t need) {
+  if (need == 0) return VISS_OK;
+  if (!ws) return fail(VISS_ERR_WORKSPACE, "workspace is NULL");
+  if (reinterpret_cast<uintptr_t>(ws) & 255) return fail(VISS_ERR_WORKSPACE, "workspace not 256-byte aligned");
+  if (have < need)
+    return fail(VISS_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need) + " bytes");
+  return VISS_OK;
+}
+
+// ------------------------------------------------------------------ passes
+int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
+                 const viss_vis_set& vis, const viss_geometry* geo, float* V, void* ws, size_t ws_bytes,
+                 cudaStream_t st) {
+  VisPlan p;
+  plan_vis(p, cfg, vis.K, sky.J, geo);
+  int rc = check_ws(ws, ws_bytes, p.bytes);
+  if (rc) return rc;
+  if (vis.K == 0) return VISS_OK;
+  if (sky.J == 0) {
+    VISS_CUDA(cudaMemsetAsync(V, 0, sizeof(float2) * (size_t)vis.K, st));
+    return VISS_OK;
+  }
+  if (p.plain) return launch_vis_plain(cfg, sky, vis, geo, dlmn, reinterpret_cast<float2*>(V), st);
+  p.layout(ws);
+  VISS_CUDA(cudaMemsetAsync(p.flags, 0, 64 * sizeof(int), st));
+  PixPrepArgs pa{};
+  pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = sky.bright;
+  pa.J = sky.J; pa.Jpad = p.Jpad;
+  pa.sl = scale[0]; pa.sm = scale[1]; pa.sn = scale[2]; pa.n_offset = cfg.n_offset;
+  pa.res = cfg.res; pa.trunc = cfg.trunc_brightness;
+  pa.rec0 = p.pix0; pa.rec1 = p.pix1; pa.lo = p.plo; pa.geo = p.pgeo; pa.qr = p.pqr;
+  if ((rc = launch_prep_pixels(pa, st))) return rc;
+  RowPrepArgs ra{};
+  ra.u = vis.u; ra.v = vis.v; ra.w = vis.w; ra.shade = vis.shade;
+  ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
+  ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
+  ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = cfg.mask_mode; ra.recon_mask = VISS_RECON_MASK_NONE;
+  ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.flags = p.flags;
+  if ((rc = launch_prep_rows(ra, false, st))) return rc;
+  if (p.geo) {
+    if ((rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
+    if ((rc = launch_prep_rowblock_cones(p.rows0, p.rows1, p.satdir, vis.K, VIS_ROWS, p.nrb, p.cones, st)))
+      return rc;
+  }
+  VisParams vp{};
+  vp.pix0 = p.pix0; vp.pix1 = p.pix1; vp.plo = p.plo; vp.pgeo = p.pgeo; vp.pqr = p.pqr;
+  vp.rows0 = p.rows0; vp.rows1 = p.rows1; vp.rowsf = p.rowsf; vp.win = p.win;
+  vp.satdir = p.satdir; vp.cones = p.cones;
+  vp.l = sky.l; vp.m = sky.m; vp.n = sky.n; vp.sat_pos = geo ? geo->sat_pos : nullptr;
+  vp.flags = p.flags;
+  vp.out = p.nsplit > 1 ? p.partial : reinterpret_cast<float2*>(V);
+  vp.K = vis.K; vp.J = sky.J; vp.jchunk = p.jchunk; vp.nsplit = p.nsplit;
+  vp.res = cfg.res > 0 ? cfg.res : 1; vp.occ_val = cfg.occluded_value; vp.R = cfg.moon_radius_km;
+  vp.mask = cfg.mask_mode;
+  if ((rc = launch_vis_fast(vp, p.nrb, p.comp, st))) return rc;
+  if (p.nsplit > 1) return launch_vis_reduce(p.partial, p.nsplit, vis.K, reinterpret_cast<float2*>(V), st);
+  return VISS_OK;
+}
+
+int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
+               const viss_vis_set& vis, const viss_geometry* geo, const float* V, float* F, void* ws,
+               size_t ws_bytes, cudaStream_t st, const float* ratio_arrays[4]) {
+  RecPlan p;
+  plan_recon(p, cfg, vis.K, sky.J, geo);
+  int rc = check_ws(ws, ws_bytes, p.bytes);
+  if (rc) return rc;
+  if (sky.J == 0) return VISS_OK;
+  if (vis.K == 0) {
+    VISS_CUDA(cudaMemsetAsync(F, 0, sizeof(float2) * (size_t)sky.J, st));
+    return VISS_OK;
+  }
+  p.layout(ws);
+  VISS_CUDA(cudaMemsetAsync(p.flags, 0, 64 * sizeof(int), st));
+  if (p.plain) {
+    const float* ratios = nullptr;
+    if (p.ref) {
+      if (ratio_arrays) {
+        VISS_CUDA(cudaMemcpyAsync(p.ratios, ratio_arrays[0], sizeof(float) * vis.K, cudaMemcpyDeviceToDevice, st));
+        VISS_CUDA(cudaMemcpyAsync(p.ratios + vis.K, ratio_arrays[1], sizeof(float) * vis.K,
+                                  cudaMemcpyDeviceToDevice, st));
+      } else {
+        extern int launch_shade_ratios(const int32_t* shade, int64_t K, float* r, cudaStream_t st);
+        if ((rc = launch_shade_ratios(vis.shade, vis.K, p.ratios, st))) return rc;
+      }
+      ratios = p.ratios;
+    }
+    return launch_recon_plain(cfg, sky, vis, geo, V, ratios, dlmn, reinterpret_cast<float2*>(F), st);
+  }
+  PixPrepArgs pa{};
+  pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = nullptr;
+  pa.J = sky.J; pa.Jpad = p.Jpad;
+  pa.sl = scale[0]; pa.sm = scale[1]; pa.sn = scale[2]; pa.n_offset = cfg.n_offset;
+  pa.res = cfg.res; pa.trunc = 0;
+  pa.rec0 = p.pix0; pa.rec1 = p.pix1; pa.lo = p.plo; pa.geo = p.pgeo; pa.qr = p.pqr;
+  if ((rc = launch_prep_pixels(pa, st))) return rc;
+  RowPrepArgs ra{};
+  ra.u = vis.u; ra.v = vis.v; ra.w = vis.w; ra.wgt = vis.wgt; ra.V = V;
+  ra.shade = ratio_arrays ? nullptr : vis.shade;
+  ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
+  ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
+  ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = VISS_MASK_NONE; ra.recon_mask = cfg.recon_mask;
+  ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.y = p.y; ra.flags = p.flags;
+  if ((rc = launch_prep_rows(ra, true, st))) return rc;
+  if (p.ref && ratio_arrays) {
+    if ((rc = launch_prep_recon_ratios(ratio_arrays[0], ratio_arrays[1], ratio_arrays[2], ratio_arrays[3], vis.K,
+                                       p.Kpad, p.win, p.flags, st)))
+      return rc;
+  }
+  if (p.geo) {
+    if ((rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
+    if ((rc = launch_prep_snapshot_cones(p.satdir, geo->S, geo->nsat, p.scones, st))) return rc;
+  }
+  ReconParams rp{};
+  rp.pix0 = p.pix0; rp.pix1 = p.pix1; rp.plo = p.plo; rp.pgeo = p.pgeo; rp.pqr = p.pqr;
+  rp.rows0 = p.rows0; rp.rows1 = p.rows1; rp.rowsf = p.rowsf; rp.win = p.win; rp.y = p.y;
+  rp.satdir = p.satdir; rp.scones = p.scones;
+  rp.l = sky.l; rp.m = sky.m; rp.n = sky.n; rp.sat_pos = geo ? geo->sat_pos : nullptr;
+  rp.flags = p.flags;
+  rp.out = p.nsplit > 1 ? p.partial : reinterpret_cast<float2*>(F);
+  rp.K = vis.K; rp.J = sky.J; rp.kchunk = p.kchunk; rp.nsplit = p.nsplit;
+  rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
+  rp.norm = (float)cfg.norm; rp.recon_mask = cfg.recon_mask;
+  if ((rc = launch_recon_fast(rp, p.npb, p.comp, st))) return rc;
+  if (p.nsplit > 1)
+    return launch_recon_reduce(p.partial, p.nsplit, sky.J, (float)cfg.norm, reinterpret_cast<float2*>(F), st);
+  return VISS_OK;
+}
+
+// SoA shade columns -> K x 4
+__global__ void pack_shade_kernel(const int* M1, const int* M2, const int* M3, const int* M4, int64_t K, int4* out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < K) out[k] = make_int4(M1[k], M2[k], M3[k], M4[k]);
+}
+
+__global__ void shade_ratios_kernel(const int32_t* shade, int64_t K, float* r) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  r[k] = (float)shade[4 * k] / (float)shade[4 * k + 1];
+  r[K + k] = (float)shade[4 * k + 2] / (float)shade[4 * k + 3];
+}
+
+int launch_shade_ratios(const int32_t* shade, int64_t K, float* r, cudaStream_t st) {
+  if (K <= 0) return VISS_OK;
+  shade_ratios_kernel<<<(unsigned)((K + 255) / 256), 256, 0, st>>>(shade, K, r);
+  VISS_LAUNCH_CHECK("shade_ratios_kernel");
+  return VISS_OK;
+}
+
+}  // namespace viss
+
+using namespace viss;
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char* viss_status_str(int status) {
+  switch (status) {
+    case VISS_OK: return "ok";
+    case VISS_ERR_INVALID: return "invalid argument";
+    case VISS_ERR_WORKSPACE: return "workspace missing, misaligned or too small";
+    case VISS_ERR_CUDA: return "CUDA runtime error";
+    case VISS_ERR_RANGE: return "input out of supported range";
+    case VISS_ERR_TIMEOUT: return "device-side wait timed out";
+    case VISS_ERR_UNSUPPORTED: return "unsupported combination";
+    case VISS_ERR_IO: return "file I/O error";
+    case VISS_ERR_FORMAT: return "file format error";
+    default: return "unknown status";
+  }
+}
+
+const char* viss_last_error(void) { return g_last_error.c_str(); }
+
+int viss_version(void) { return 10000; }
+
+uint64_t viss_launch_count(void) { return g_launches; }
+
+size_t viss_vis_dft_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo) {
+  if (!cfg) return 0;
+  VisPlan p;
+  plan_vis(p, *cfg, K, J, geo);
+  return p.bytes;
+}
+
+int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis, const viss_geometry* geo,
+                 float* V, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc;
+  if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, true)) || (rc = check_vis(vis))) return rc;
+  if (vis->K > 0 && !V) return fail(VISS_ERR_INVALID, "V is NULL");
+  if ((cfg->mask_mode == VISS_MASK_REF_QUIRK || cfg->mask_mode == VISS_MASK_REF_INTENDED)) {
+    if (!vis->shade) return fail(VISS_ERR_INVALID, "REF mask needs shade windows");
+    if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF mask needs res >= 1");
+  }
+  if (cfg->mask_mode == VISS_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  const double s = cfg->phase_scale;
+  const double scale[3] = {s, s, s};
+  const float d = (float)(1.0 / s);
+  const float dlmn[3] = {d, d, d};
+  return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, geo, V, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream));
+}
+
+size_t viss_recon_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo) {
+  if (!cfg) return 0;
+  RecPlan p;
+  plan_recon(p, *cfg, K, J, geo);
+  return p.bytes;
+}
+
+int viss_recon(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis, const viss_geometry* geo,
+               const float* V, float* F, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc;
+  if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, false)) || (rc = check_vis(vis))) return rc;
+  if (sky->J > 0 && !F) return fail(VISS_ERR_INVALID, "F is NULL");
+  if (vis->K > 0 && !V) return fail(VISS_ERR_INVALID, "V is NULL");
+  if (cfg->recon_mask == VISS_RECON_MASK_REF) {
+    if (!vis->shade) return fail(VISS_ERR_INVALID, "REF recon mask needs shade windows");
+    if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF recon mask needs res >= 1");
+  }
+  if (cfg->recon_mask == VISS_RECON_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  const double s = cfg->phase_scale;
+  const double scale[3] = {s, s, s};
+  const float d = (float)(1.0 / s);
+  const float dlmn[3] = {d, d, d};
+  return recon_impl(*cfg, scale, dlmn, *sky, *vis, geo, V, F, workspace, workspace_bytes,
+                    static_cast<cudaStream_t>(stream), nullptr);
+}
+
+int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float* viss, const float* u,
+                 const float* v, const float* w, const float* l, const float* m, const float* n, const int* shadeM1,
+                 const int* shadeM2, const int* shadeM3, const int* shadeM4, const float* NXq, const int* countLoc,
+                 float dl, float dm, float dn, int variant, int mask_mode, int precision, void* stream) {
+  if (uvws_index < 0 || lmnC_index < 0) return fail(VISS_ERR_RANGE, "negative size");
+  if (NXq || countLoc)
+    return fail(VISS_ERR_UNSUPPORTED, "non-identity fine->coarse map (NXq/countLoc) is not supported here");
+  if (!(dl > 0.f && dm > 0.f && dn > 0.f)) return fail(VISS_ERR_RANGE, "dl, dm, dn must be > 0");
+  if (mask_mode != VISS_MASK_NONE && mask_mode != VISS_MASK_REF_QUIRK && mask_mode != VISS_MASK_REF_INTENDED)
+    return fail(VISS_ERR_INVALID, "viss_visscal takes NONE or a REF mask");
+  if (mask_mode != VISS_MASK_NONE && (!shadeM1 || !shadeM2 || !shadeM3 || !shadeM4))
+    return fail(VISS_ERR_INVALID, "shadeM arrays NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  viss_dft_cfg cfg{};
+  cfg.mask_mode = mask_mode;
+  cfg.recon_mask = VISS_RECON_MASK_NONE;
+  cfg.precision = precision;
+  cfg.res = res;
+  cfg.trunc_brightness = variant == VISS_VARIANT_PLAIN ? 1 : 0;
+  cfg.occluded_value = 240.0f;  // vissGen10M_shade.cu:132
+  cfg.phase_scale = 1.0 / dl;
+  cfg.n_offset = 0.0;           // w(n-1) inside, e^{-2 pi i w/dn} outside (:137-143)
+  cfg.moon_radius_km = 1737.4;
+  cfg.norm = 1.0;
+  int rc = check_cfg(&cfg);
+  if (rc) return rc;
+  viss_sky sky{l, m, n, FF, lmnC_index};
+  viss_vis_set vis{u, v, w, nullptr, nullptr, nullptr, nullptr, uvws_index};
+  const double scale[3] = {1.0 / dl, 1.0 / dm, 1.0 / dn};
+  const float dlmn[3] = {dl, dm, dn};
+  VisPlan p;
+  plan_vis(p, cfg, uvws_index, lmnC_index, nullptr);
+  const size_t shade_bytes = mask_mode != VISS_MASK_NONE ? ((sizeof(int4) * (size_t)uvws_index + 255) & ~size_t(255)) : 0;
+  void* ws = nullptr;
+  const size_t total = p.bytes + shade_bytes;
+  if (total) VISS_CUDA(cudaMallocAsync(&ws, total, st));
+  if (shade_bytes && uvws_index > 0) {
+    int4* packed = reinterpret_cast<int4*>(static_cast<char*>(ws) + p.bytes);
+    pack_shade_kernel<<<(unsigned)((uvws_index + 255) / 256), 256, 0, st>>>(shadeM1, shadeM2, shadeM3, shadeM4,
+                                                                            uvws_index, packed);
+    VISS_LAUNCH_CHECK("pack_shade_kernel");
+    vis.shade = reinterpret_cast<const int32_t*>(packed);
+  }
+  rc = vis_dft_impl(cfg, scale, dlmn, sky, vis, nullptr, viss, ws, p.bytes, st);
+  if (ws) {
+    cudaError_t e = cudaFreeAsync(ws, st);
+    if (rc == VISS_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaFreeAsync");
+  }
+  return rc;
+}
+
+int viss_imagerecon(int uvw_index, int lmnC_index, int res, float* F, const float* viss, const float* u,
+                    const float* v, const float* w, const float* l, const float* m, const float* n,
+                    const float* uvwFrequencyMap, const float* thetaP0, const float* phiP0, const float* dtheta,
+                    const float* dphi, float dl, float dm, float dn, int precision, void* stream) {
+  if (uvw_index < 0 || lmnC_index < 0) return fail(VISS_ERR_RANGE, "negative size");
+  if (!(dl > 0.f && dm > 0.f && dn > 0.f)) return fail(VISS_ERR_RANGE, "dl, dm, dn must be > 0");
+  const bool masked = thetaP0 && phiP0 && dtheta && dphi;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  viss_dft_cfg cfg{};
+  cfg.mask_mode = VISS_MASK_NONE;
+  cfg.recon_mask = masked ? VISS_RECON_MASK_REF : VISS_RECON_MASK_NONE;
+  cfg.precision = precision;
+  cfg.res = res;
+  cfg.occluded_value = 0.f;
+  cfg.phase_scale = 1.0 / dl;
+  cfg.n_offset = 0.0;  // w*n/dn (:169)
+  cfg.moon_radius_km = 1737.4;
+  cfg.norm = uvw_index > 0 ? 1.0 / (double)uvw_index : 1.0;  // F / amount (:174)
+  int rc = check_cfg(&cfg);
+  if (rc) return rc;
+  if (masked && res < 1) return fail(VISS_ERR_RANGE, "res must be >= 1");
+  viss_sky sky{l, m, n, nullptr, lmnC_index};
+  viss_vis_set vis{u, v, w, uvwFrequencyMap, nullptr, nullptr, nullptr, uvw_index};
+  const double scale[3] = {1.0 / dl, 1.0 / dm, 1.0 / dn};
+  const float dlmn[3] = {dl, dm, dn};
+  RecPlan p;
+  plan_recon(p, cfg, uvw_index, lmnC_index, nullptr);
+  void* ws = nullptr;
+  if (p.bytes) VISS_CUDA(cudaMallocAsync(&ws, p.bytes, st));
+  const float* ratios[4] = {thetaP0, phiP0, dtheta, dphi};
+  rc = recon_impl(cfg, scale, dlmn, sky, vis, nullptr, viss, F, ws, p.bytes, st, masked ? ratios : nullptr);
+  if (rc == VISS_OK && masked && precision != VISS_PREC_PLAIN) {
+    // rows whose ratio arrays are not of the reference's form are rejected
+    int flags[2] = {0, 0};
+    p.layout(ws);
+    cudaError_t e = cudaMemcpyAsync(flags, p.flags, sizeof(flags), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_fail(e, "flag readback");
+    else if (flags[1] & 4) rc = fail(VISS_ERR_UNSUPPORTED, "thetaP0 != dtheta or phiP0 != dphi");
+  }
+  if (ws) {
+    cudaError_t e = cudaFreeAsync(ws, st);
+    if (rc == VISS_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaFreeAsync");
+  }
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,319 @@
+// prep.cu -- per-pass preparation kernels: fixed-point pixel and visibility
+// records, satellite directions and occlusion cones.  All O(J + K + S*nsat);
+// the O(K*J) work is in vis_dft.cu and recon.cu.
+#include <cfloat>
+
+#include "viss_internal.cuh"
+
+namespace viss {
+
+// ------------------------------------------------------------- pixels
+// Pixel j: phase coordinates x = s*l, y = s*m, z = s*(n + n_offset) in turns per
+// wavelength, evaluated in double from the float inputs.
+__global__ void prep_pixels_kernel(PixPrepArgs a) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.Jpad) return;
+  if (j >= a.J) {
+    a.rec0[j] = make_int4(0, 0, 0, 0);
+    if (a.rec1) a.rec1[j] = make_int4(0, 0, 0, (int)j);
+    if (a.lo) a.lo[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.geo) a.geo[j] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)j));
+    if (a.qr) a.qr[j] = make_int2(-1, -1);
+    return;
+  }
+  const double x = a.sl * (double)a.l[j];
+  const double y = a.sm * (double)a.m[j];
+  const double z = a.sn * ((double)a.n[j] + a.n_offset);
+  float b = 0.f;
+  if (a.bright) {
+    b = a.bright[j];
+    if (a.trunc) b = (float)(int)b;  // int addFF = FF[..] (vissGen10M_shade.cu:128)
+  }
+  const uint32_t A = fix32(x), B = fix32(y), C = fix32(z);
+  a.rec0[j] = make_int4((int)A, (int)B, (int)C, __float_as_int(b));
+  if (a.rec1) {
+    a.rec1[j] = make_int4((int)llrint(x * 1073741824.0), (int)llrint(y * 1073741824.0),
+                          (int)llrint(z * 1073741824.0), (int)j);
+  }
+  if (a.lo) {
+    const double sc = 4294967296.0;
+    const double xa = x * sc, ya = y * sc, za = z * sc;
+    a.lo[j] = make_float4((float)((xa - rint(xa)) / sc), (float)((ya - rint(ya)) / sc),
+                          (float)((za - rint(za)) / sc), 0.f);
+  }
+  if (a.geo) {
+    const double gx = a.l[j], gy = a.m[j], gz = a.n[j];
+    const double nn = sqrt(gx * gx + gy * gy + gz * gz);
+    const double inv = nn > 0 ? 1.0 / nn : 0.0;
+    a.geo[j] = make_float4((float)(gx * inv), (float)(gy * inv), (float)(gz * inv), __int_as_float((int)j));
+  }
+  if (a.qr) {
+    const int res = a.res > 0 ? a.res : 1;
+    a.qr[j] = make_int2((int)(j / res), (int)(j % res));
+  }
+}
+
+int launch_prep_pixels(const PixPrepArgs& a, cudaStream_t st) {
+  if (a.Jpad <= 0) return VISS_OK;
+  const int bs = 256;
+  prep_pixels_kernel<<<(unsigned)((a.Jpad + bs - 1) / bs), bs, 0, st>>>(a);
+  VISS_LAUNCH_CHECK("prep_pixels_kernel");
+  return VISS_OK;
+}
+
+// ------------------------------------------------------------- rows
+// Reference recon mask (vissGen10M_shade.cu:166): skip iff
+//   fabsf(r1 - thetaP) < r1 && fabsf(r2 - phiP) < r2,  r = (float)Ma / (float)Mb
+// with thetaP, phiP non-negative integers.  The set of integers t passing the
+// first test is {1..tmax} (empty when r1 <= 0 or NaN); tmax is found from the
+// exact float predicate.
+__device__ int recon_ratio_tmax(float r) {
+  if (!(r > 0.f) || isinf(r)) return 0;
+  // candidates t < 2r; find the largest t >= 1 with fabsf(r - t) < r
+  double lim = 2.0 * (double)r;
+  long long t = (long long)ceil(lim) - 1;
+  if (t > 2147483000LL) t = 2147483000LL;
+  for (long long c = t + 1; c >= t - 1 && c >= 1; --c) {
+    if (fabsf(r - (float)c) < r) return (int)c;
+  }
+  return 0;
+}
+
+__global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.Kpad) return;
+  if (k >= a.K) {
+    a.rec0[k] = make_int4(0, 0, 0, 0);
+    a.rec1[k] = make_int4(0, 0, 0, 0);
+    if (a.uf) a.uf[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.win) a.win[k] = make_int4(1, 0, 0, 0);
+    if (a.y) a.y[k] = make_float2(0.f, 0.f);
+    return;
+  }
+  const double uu = a.u[k], vv = a.v[k], ww = a.w[k];
+  const double Uu = floor(uu + 0.5), Uv = floor(vv + 0.5), Uw = floor(ww + 0.5);
+  const double lim = 1073741824.0;  // |U| < 2^30
+  if (!(fabs(Uu) < lim && fabs(Uv) < lim && fabs(Uw) < lim)) atomicOr(a.flags + 1, 1);
+  const int Fu = (int)llrint((uu - Uu) * 4294967296.0);
+  const int Fv = (int)llrint((vv - Uv) * 4294967296.0);
+  const int Fw = (int)llrint((ww - Uw) * 4294967296.0);
+  if (Fu | Fv | Fw) atomicOr(a.flags, 1);
+  int gm = 0, gn = 0;
+  if (a.snap && a.pair) {
+    const int s = a.snap[k];
+    const int pr = a.pair[k];
+    const int pm = pr & 0xffff, pn = (pr >> 16) & 0xffff;
+    if (s < 0 || s >= a.S || pm >= a.nsat || pn >= a.nsat) {
+      atomicOr(a.flags + 1, 2);
+    } else {
+      gm = s * a.nsat + pm;
+      gn = s * a.nsat + pn;
+    }
+  }
+  a.rec0[k] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, gm);
+  a.rec1[k] = make_int4(Fu, Fv, Fw, gn);
+  if (a.uf) a.uf[k] = make_float4((float)Uu, (float)Uv, (float)Uw, 0.f);
+  if (a.win) {
+    int4 wv = make_int4(1, 0, 0, 0);  // empty
+    if (a.shade) {
+      const int M1 = a.shade[4 * k], M2 = a.shade[4 * k + 1], M3 = a.shade[4 * k + 2],
+                M4 = a.shade[4 * k + 3];
+      if (!recon) {
+        if (a.mask_mode == VISS_MASK_REF_QUIRK) {
+          if (M3 <= 0 && M4 >= 0) wv = make_int4(0, M4, M1, M2);
+        } else if (a.mask_mode == VISS_MASK_REF_INTENDED) {
+          if (M3 <= M4) wv = make_int4(M3, M4, M1, M2);
+        }
+      } else if (a.recon_mask == VISS_RECON_MASK_REF) {
+        const float r1 = (float)M1 / (float)M2, r2 = (float)M3 / (float)M4;
+        wv = make_int4(recon_ratio_tmax(r1), recon_ratio_tmax(r2), 0, 0);
+      }
+    }
+    a.win[k] = wv;
+  }
+  if (a.y) {
+    const float wg = a.wgt ? a.wgt[k] : 1.0f;
+    a.y[k] = make_float2(wg * a.V[2 * k], wg * a.V[2 * k + 1]);
+  }
+}
+
+int launch_prep_rows(const RowPrepArgs& a, bool recon, cudaStream_t st) {
+  if (a.Kpad <= 0) return VISS_OK;
+  const int bs = 256;
+  prep_rows_kernel<<<(unsigned)((a.Kpad + bs - 1) / bs), bs, 0, st>>>(a, recon);
+  VISS_LAUNCH_CHECK("prep_rows_kernel");
+  return VISS_OK;
+}
+
+// Reference recon ratio arrays given directly (viss_imagerecon): same tmax rule.
+__global__ void prep_recon_ratios_kernel(const float* thetaP0, const float* phiP0, const float* dtheta,
+                                         const float* dphi, int64_t K, int64_t Kpad, int4* win,
+                                         int* flags) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= Kpad) return;
+  if (k >= K) { win[k] = make_int4(0, 0, 0, 0); return; }
+  // skip iff fabsf(t0 - thetaP) < dt && fabsf(p0 - phiP) < dp.  The reference
+  // passes the same ratio array twice (t0 == dt, p0 == dp, :514-517); rows
+  // of another form set flag bit 4 and the call is rejected.
+  const float t0 = thetaP0[k], dt = dtheta[k], p0 = phiP0[k], dp = dphi[k];
+  const bool same_t = (t0 == dt) || (t0 != t0 && dt != dt);
+  const bool same_p = (p0 == dp) || (p0 != p0 && dp != dp);
+  if (!same_t || !same_p) atomicOr(flags + 1, 4);
+  win[k] = make_int4(recon_ratio_tmax(t0), recon_ratio_tmax(p0), 0, 0);
+}
+
+// ------------------------------------------------------------- satellites
+// satdir[i] = {p/|p|, cos(alpha)}, alpha = asin(R/|p|) the Moon's angular radius
+// seen from the satellite.  Occluded <=> s_hat . p_hat < -cos(alpha).  A
+// satellite inside the sphere (|p| <= R) gets cos(alpha) = 0 (occluded <=> s.p < 0),
+// which is what the exact predicate gives there.
+__global__ void prep_satdir_kernel(const float* pos, int64_t nsd, double R, float4* satdir) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsd) return;
+  const double px = pos[3 * i], py = pos[3 * i + 1], pz = pos[3 * i + 2];
+  const double r = sqrt(px * px + py * py + pz * pz);
+  if (!(r > 0.0)) {
+    satdir[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const double ca = r > R ? sqrt(1.0 - (R / r) * (R / r)) : 0.0;
+  satdir[i] = make_float4((float)(px / r), (float)(py / r), (float)(pz / r), (float)ca);
+}
+
+int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satdir, cudaStream_t st) {
+  if (nsd <= 0) return VISS_OK;
+  prep_satdir_kernel<<<(unsigned)((nsd + 255) / 256), 256, 0, st>>>(sat_pos, nsd, R, satdir);
+  VISS_LAUNCH_CHECK("prep_satdir_kernel");
+  return VISS_OK;
+}
+
+// ------------------------------------------------------------- cones
+// For a set of satellites {p_i} with shadow cones (axis -p_hat_i, half angle
+// alpha_i): axis c = normalise(sum -p_hat_i), rho = max angle(c, -p_hat_i).
+// A pixel s_hat with s_hat.c > cos(alpha_min - rho - eps) is occluded for every
+// satellite of the set; with s_hat.c < cos(alpha_max + rho + eps) it is visible
+// from every one.  cone[0] = {c, cos_occ}, cone[1] = {cos_vis, -, -, -}.
+// Degenerate sets (a satellite at the origin) get cos_occ = 2, cos_vis = -2.
+// Block-wide: one block per cone; members enumerated by `member(i)` -> satdir index.
+template <class Member>
+__device__ void cone_block(const float4* satdir, int64_t count, Member member, float4* out) {
+  __shared__ double red[4][32];
+  __shared__ double axis[3];
+  __shared__ int degen_s;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  if (tid == 0) degen_s = 0;
+  __syncthreads();
+  double sx = 0, sy = 0, sz = 0;
+  for (int64_t i = tid; i < count; i += blockDim.x) {
+    const float4 d = satdir[member(i)];
+    if (d.x == 0.f && d.y == 0.f && d.z == 0.f) { atomicOr(&degen_s, 1); continue; }
+    if (d.w == 0.f) atomicOr(&degen_s, 1);  // inside the sphere: no cone
+    sx -= d.x; sy -= d.y; sz -= d.z;
+  }
+  for (int o = 16; o; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
+  }
+  if (lane == 0) { red[0][wid] = sx; red[1][wid] = sy; red[2][wid] = sz; }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0, b = 0, c = 0;
+    for (int w = 0; w < nw; ++w) { a += red[0][w]; b += red[1][w]; c += red[2][w]; }
+    const double nn = sqrt(a * a + b * b + c * c);
+    axis[0] = nn > 0 ? a / nn : 0; axis[1] = nn > 0 ? b / nn : 0; axis[2] = nn > 0 ? c / nn : 1;
+    if (!(nn > 0)) degen_s = 1;
+  }
+  __syncthreads();
+  // rho (as min cos), alpha range
+  double mincos = 2.0, amin = 10.0, amax = -1.0;
+  for (int64_t i = tid; i < count; i += blockDim.x) {
+    const float4 d = satdir[member(i)];
+    const double c = -(axis[0] * d.x + axis[1] * d.y + axis[2] * d.z);
+    mincos = fmin(mincos, c);
+    const double al = acos(fmin(1.0, fmax(-1.0, (double)d.w)));
+    amin = fmin(amin, al);
+    amax = fmax(amax, al);
+  }
+  for (int o = 16; o; o >>= 1) {
+    mincos = fmin(mincos, __shfl_xor_sync(0xffffffffu, mincos, o));
+    amin = fmin(amin, __shfl_xor_sync(0xffffffffu, amin, o));
+    amax = fmax(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  }
+  __syncthreads();
+  if (lane == 0) { red[0][wid] = mincos; red[1][wid] = amin; red[2][wid] = amax; }
+  __syncthreads();
+  if (tid == 0) {
+    double mc = 2.0, a0 = 10.0, a1 = -1.0;
+    for (int w = 0; w < nw; ++w) { mc = fmin(mc, red[0][w]); a0 = fmin(a0, red[1][w]); a1 = fmax(a1, red[2][w]); }
+    const double eps = 1e-5;
+    float cos_occ = 2.f, cos_vis = -2.f;
+    if (!degen_s && count > 0) {
+      const double rho = acos(fmin(1.0, fmax(-1.0, mc)));
+      const double lo = a0 - rho - eps, hi = a1 + rho + eps;
+      if (lo > 0) cos_occ = (float)cos(lo);
+      if (hi < kPi) cos_vis = (float)cos(hi);
+      // widen by float rounding of the test s_hat . c
+      if (cos_occ <= 1.f) cos_occ = fminf(2.f, cos_occ + 1e-6f);
+      if (cos_vis >= -1.f) cos_vis = cos_vis - 1e-6f;
+    }
+    out[0] = make_float4((float)axis[0], (float)axis[1], (float)axis[2], cos_occ);
+    out[1] = make_float4(cos_vis, 0.f, 0.f, 0.f);
+  }
+}
+
+struct RowMember {
+  const int4* rows0;
+  const int4* rows1;
+  int64_t base;
+  __device__ int operator()(int64_t i) const {
+    const int64_t k = base + (i >> 1);
+    return (i & 1) ? rows1[k].w : rows0[k].w;
+  }
+};
+
+__global__ void rowblock_cones_kernel(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
+                                      int rows_per_block, float4* cones) {
+  const int64_t b = blockIdx.x;
+  const int64_t base = b * rows_per_block;
+  int64_t cnt = K - base;
+  if (cnt > rows_per_block) cnt = rows_per_block;
+  if (cnt < 0) cnt = 0;
+  cone_block(satdir, 2 * cnt, RowMember{rows0, rows1, base}, cones + 2 * b);
+}
+
+int launch_prep_rowblock_cones(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
+                               int rows_per_block, int64_t nblocks, float4* cones, cudaStream_t st) {
+  if (nblocks <= 0) return VISS_OK;
+  rowblock_cones_kernel<<<(unsigned)nblocks, 256, 0, st>>>(rows0, rows1, satdir, K, rows_per_block, cones);
+  VISS_LAUNCH_CHECK("rowblock_cones_kernel");
+  return VISS_OK;
+}
+
+struct SnapMember {
+  int64_t base;
+  __device__ int operator()(int64_t i) const { return (int)(base + i); }
+};
+
+__global__ void snapshot_cones_kernel(const float4* satdir, int nsat, float4* cones) {
+  const int64_t s = blockIdx.x;
+  cone_block(satdir, nsat, SnapMember{s * nsat}, cones + 2 * s);
+}
+
+int launch_prep_snapshot_cones(const float4* satdir, int64_t S, int nsat, float4* cones, cudaStream_t st) {
+  if (S <= 0) return VISS_OK;
+  snapshot_cones_kernel<<<(unsigned)S, 32, 0, st>>>(satdir, nsat, cones);
+  VISS_LAUNCH_CHECK("snapshot_cones_kernel");
+  return VISS_OK;
+}
+
+int launch_prep_recon_ratios(const float* thetaP0, const float* phiP0, const float* dtheta, const float* dphi,
+                             int64_t K, int64_t Kpad, int4* win, int* flags, cudaStream_t st) {
+  if (Kpad <= 0) return VISS_OK;
+  prep_recon_ratios_kernel<<<(unsigned)((Kpad + 255) / 256), 256, 0, st>>>(thetaP0, phiP0, dtheta, dphi, K,
+                                                                          Kpad, win, flags);
+  VISS_LAUNCH_CHECK("prep_recon_ratios_kernel");
+  return VISS_OK;
+}
+
+}  // namespace viss

@@ -1,0 +1,354 @@
+// recon.cu -- direct-DFT reconstruction (replaces imagerecon, vissGen10M_shade.cu:149-175,
+// and the tiled optim2 form, vissGen10M_shade_optim2.cu:219-317).
+//
+// F_j = norm * sum_k [not masked] y_k exp(+2 pi i t_kj),  y_k = wgt_k V_k
+//
+// A CTA owns REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates in
+// registers) and streams visibility records (uvw fixed point + y) through
+// shared memory in tiles of REC_Q.  Per term: 3 IMAD [+fractional, +compensated
+// terms as in the vis kernel], turns -> angle, __sincosf, 4 FFMA.
+// Masks:
+//   GEOMETRIC: rows come in snapshot runs; per run every thread tests its pixels
+//     against the snapshot's bounding cone and the warp votes: all occluded ->
+//     the run is skipped, all visible -> unmasked loop, else the thread builds a
+//     per-pixel satellite occlusion bitmask and tests each row's pair.
+//   REF: the reference ratio mask can only fire on pixels (thetaP, phiP) with
+//     1 <= thetaP <= tmax_k, 1 <= phiP <= pmax_k; tiles whose rows cannot touch
+//     the CTA's pixels run unmasked.
+// Visibility chunks (blockIdx.y) give partial sums, reduced in a fixed order.
+#include "viss_internal.cuh"
+
+namespace viss {
+
+template <bool FRAC, bool COMP>
+__device__ __forceinline__ void rec_term(const int4& r0, const int4& r1, const float4& rf, float2 y, int A, int B,
+                                         int C, int Ap, int Bp, int Cp, float lx, float ly, float lz, float& fr,
+                                         float& fi) {
+  uint32_t q = (uint32_t)r0.x * (uint32_t)A + (uint32_t)r0.y * (uint32_t)B + (uint32_t)r0.z * (uint32_t)C +
+               (uint32_t)PHASE_BIAS;
+  if (FRAC) {
+    const uint32_t h = (uint32_t)mulhi(r1.x, Ap) + (uint32_t)mulhi(r1.y, Bp) + (uint32_t)mulhi(r1.z, Cp);
+    q += h << 2;
+  }
+  float x = turns_to_angle(q);
+  if (COMP) {
+    const float d = fmaf(rf.x, lx, fmaf(rf.y, ly, rf.z * lz));
+    x = fmaf(d, K2PI, x);
+  }
+  float sn, cs;
+  __sincosf(x, &sn, &cs);
+  fr = fmaf(y.x, cs, fr);
+  fr = fmaf(-y.y, sn, fr);
+  fi = fmaf(y.x, sn, fi);
+  fi = fmaf(y.y, cs, fi);
+}
+
+constexpr int RM_NONE = 0, RM_REF = 1, RM_GEO = 2;
+
+template <int RM, bool COMP>
+struct RecSmem {
+  int4 r0[REC_Q];
+  int4 r1[REC_Q];
+  float4 rf[COMP ? REC_Q : 1];
+  float2 y[REC_Q];
+  int4 win[RM == RM_REF ? REC_Q : 1];
+  int snap[RM == RM_GEO ? REC_Q : 1];
+  int runend[RM == RM_GEO ? REC_Q : 1];
+};
+
+template <int RM, bool FRAC, bool COMP>
+__device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm) {
+  const int tid = threadIdx.x;
+  const int64_t j0 = (int64_t)blockIdx.x * REC_PIX;
+  int A[REC_TJ], B[REC_TJ], C[REC_TJ], Ap[REC_TJ], Bp[REC_TJ], Cp[REC_TJ];
+  float LX[REC_TJ], LY[REC_TJ], LZ[REC_TJ];
+  float GX[REC_TJ], GY[REC_TJ], GZ[REC_TJ];
+  int TP[REC_TJ], PP[REC_TJ], JJ[REC_TJ];
+  float fr[REC_TJ], fi[REC_TJ];
+#pragma unroll
+  for (int i = 0; i < REC_TJ; ++i) {
+    const int64_t j = j0 + tid + i * REC_THREADS;  // pixels padded to a whole block
+    JJ[i] = (int)j;
+    const int4 a = p.pix0[j];
+    A[i] = a.x; B[i] = a.y; C[i] = a.z;
+    Ap[i] = Bp[i] = Cp[i] = 0;
+    if (FRAC) { const int4 b = p.pix1[j]; Ap[i] = b.x; Bp[i] = b.y; Cp[i] = b.z; }
+    LX[i] = LY[i] = LZ[i] = 0.f;
+    if (COMP) { const float4 lo = p.plo[j]; LX[i] = lo.x; LY[i] = lo.y; LZ[i] = lo.z; }
+    GX[i] = GY[i] = GZ[i] = 0.f;
+    if (RM == RM_GEO) { const float4 g = p.pgeo[j]; GX[i] = g.x; GY[i] = g.y; GZ[i] = g.z; }
+    TP[i] = PP[i] = -1;
+    if (RM == RM_REF) { const int2 qr = p.pqr[j]; PP[i] = qr.x; TP[i] = qr.y; }
+    fr[i] = 0.f; fi[i] = 0.f;
+  }
+  const int64_t kb = (int64_t)blockIdx.y * p.kchunk;
+  int64_t ke = kb + p.kchunk;
+  if (ke > p.K) ke = p.K;
+  int64_t jlast = j0 + REC_PIX - 1;
+  if (jlast > p.J - 1) jlast = p.J - 1;
+
+  for (int64_t tile = kb; tile < ke; tile += REC_Q) {
+    const int nq = (int)((ke - tile) < REC_Q ? (ke - tile) : REC_Q);
+    __syncthreads();
+    bool hit = false;
+    for (int r = tid; r < nq; r += REC_THREADS) {
+      const int64_t k = tile + r;
+      const int4 r0 = p.rows0[k];
+      sm.r0[r] = r0;
+      if (FRAC || RM == RM_GEO) sm.r1[r] = p.rows1[k];
+      if (COMP) sm.rf[r] = p.rowsf[k];
+      sm.y[r] = p.y[k];
+      if (RM == RM_REF) {
+        const int4 wv = p.win[k];
+        sm.win[r] = wv;
+        if (wv.x >= 1 && wv.y >= 1) {
+          const int64_t lo_idx = (int64_t)p.res + 1, hi_idx = (int64_t)wv.y * p.res + wv.x;
+          if (lo_idx <= jlast && hi_idx >= j0) hit = true;
+        }
+      }
+      if (RM == RM_GEO) sm.snap[r] = r0.w / p.nsat;
+    }
+    const bool masked_tile = __syncthreads_or(hit) != 0;
+    if (RM == RM_GEO) {
+      for (int r = tid; r < nq; r += REC_THREADS) {
+        const int s = sm.snap[r];
+        if (r == 0 || sm.snap[r - 1] != s) {
+          int e = r + 1;
+          while (e < nq && sm.snap[e] == s) ++e;
+          sm.runend[r] = e;
+        }
+      }
+      __syncthreads();
+      for (int r = 0; r < nq;) {
+        const int re = sm.runend[r];
+        const int s = sm.snap[r];
+        const float4 c0 = __ldg(p.scones + 2 * (int64_t)s);
+        const float c1 = __ldg(p.scones + 2 * (int64_t)s + 1).x;
+        bool all_vis = true, all_occ = true;
+#pragma unroll
+        for (int i = 0; i < REC_TJ; ++i) {
+          const float d = fmaf(GX[i], c0.x, fmaf(GY[i], c0.y, GZ[i] * c0.z));
+          const bool valid = JJ[i] < p.J;
+          all_vis &= (!valid) || d < c1;
+          all_occ &= (!valid) || d > c0.w;
+        }
+        const bool wocc = __all_sync(0xffffffffu, all_occ);
+        const bool wvis = __all_sync(0xffffffffu, all_vis);
+        if (wocc) { r = re; continue; }
+        if (wvis) {
+#pragma unroll 2
+          for (int rr = r; rr < re; ++rr) {
+            const int4 r0 = sm.r0[rr];
+            int4 r1 = make_int4(0, 0, 0, 0);
+            float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (FRAC) r1 = sm.r1[rr];
+            if (COMP) rf = sm.rf[rr];
+            const float2 y = sm.y[rr];
+#pragma unroll
+            for (int i = 0; i < REC_TJ; ++i)
+              rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
+                                   fr[i], fi[i]);
+          }
+        } else {
+          // per-pixel satellite occlusion bits for snapshot s
+          uint32_t bits[REC_TJ];
+          const int g0 = s * p.nsat;
+#pragma unroll
+          for (int i = 0; i < REC_TJ; ++i) bits[i] = 0u;
+          for (int sat = 0; sat < p.nsat; ++sat) {
+            const float4 d = __ldg(p.satdir + g0 + sat);
+#pragma unroll
+            for (int i = 0; i < REC_TJ; ++i) {
+              const float e = fmaf(GX[i], d.x, fmaf(GY[i], d.y, fmaf(GZ[i], d.z, d.w)));
+              bool occ = e < 0.f;
+              if (fabsf(e) < GEO_EPS && JJ[i] < p.J) {
+                const int j = JJ[i];
+                occ = geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)(g0 + sat), p.R);
+              }
+              bits[i] |= (occ ? 1u : 0u) << sat;
+            }
+          }
+          for (int rr = r; rr < re; ++rr) {
+            const int4 r0 = sm.r0[rr];
+            const int4 r1 = sm.r1[rr];
+            float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (COMP) rf = sm.rf[rr];
+            const float2 y = sm.y[rr];
+            const uint32_t pm = (1u << (r0.w - g0)) | (1u << (r1.w - g0));
+#pragma unroll
+            for (int i = 0; i < REC_TJ; ++i) {
+              const float2 yy = (bits[i] & pm) ? make_float2(0.f, 0.f) : y;
+              rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
+                                   fr[i], fi[i]);
+            }
+          }
+        }
+        r = re;
+      }
+    } else if (RM == RM_REF && masked_tile) {
+      for (int rr = 0; rr < nq; ++rr) {
+        const int4 r0 = sm.r0[rr];
+        int4 r1 = make_int4(0, 0, 0, 0);
+        float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FRAC) r1 = sm.r1[rr];
+        if (COMP) rf = sm.rf[rr];
+        const float2 y = sm.y[rr];
+        const int4 wv = sm.win[rr];
+#pragma unroll
+        for (int i = 0; i < REC_TJ; ++i) {
+          const bool skip = TP[i] >= 1 && TP[i] <= wv.x && PP[i] >= 1 && PP[i] <= wv.y;
+          const float2 yy = skip ? make_float2(0.f, 0.f) : y;
+          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], fr[i],
+                               fi[i]);
+        }
+      }
+    } else {
+#pragma unroll 2
+      for (int rr = 0; rr < nq; ++rr) {
+        const int4 r0 = sm.r0[rr];
+        int4 r1 = make_int4(0, 0, 0, 0);
+        float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FRAC) r1 = sm.r1[rr];
+        if (COMP) rf = sm.rf[rr];
+        const float2 y = sm.y[rr];
+#pragma unroll
+        for (int i = 0; i < REC_TJ; ++i)
+          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], fr[i],
+                               fi[i]);
+      }
+    }
+  }
+  // F = norm * (-fr - i fi)  (the angle carried an extra half turn)
+#pragma unroll
+  for (int i = 0; i < REC_TJ; ++i) {
+    const int64_t j = j0 + tid + i * REC_THREADS;
+    if (j < p.J) {
+      if (p.nsplit == 1) p.out[j] = make_float2(-fr[i] * p.norm, -fi[i] * p.norm);
+      else p.out[(int64_t)blockIdx.y * p.J + j] = make_float2(fr[i], fi[i]);
+    }
+  }
+}
+
+template <int RM, bool COMP>
+__global__ void __launch_bounds__(REC_THREADS, 2) recon_fast_kernel(const ReconParams p) {
+  __shared__ RecSmem<RM, COMP> sm;
+  if (__ldg(p.flags) != 0) recon_body<RM, true, COMP>(p, sm);
+  else recon_body<RM, false, COMP>(p, sm);
+}
+
+template <int RM>
+static void launch_rm(const ReconParams& p, dim3 grid, bool comp, cudaStream_t st) {
+  if (comp) recon_fast_kernel<RM, true><<<grid, REC_THREADS, 0, st>>>(p);
+  else recon_fast_kernel<RM, false><<<grid, REC_THREADS, 0, st>>>(p);
+}
+
+int launch_recon_fast(const ReconParams& p, int64_t npb, bool comp, cudaStream_t st) {
+  const dim3 grid((unsigned)npb, (unsigned)p.nsplit);
+  switch (p.recon_mask) {
+    case VISS_RECON_MASK_NONE: launch_rm<RM_NONE>(p, grid, comp, st); break;
+    case VISS_RECON_MASK_REF: launch_rm<RM_REF>(p, grid, comp, st); break;
+    case VISS_RECON_MASK_GEOMETRIC: launch_rm<RM_GEO>(p, grid, comp, st); break;
+    default: return fail(VISS_ERR_INVALID, "unknown recon mask");
+  }
+  VISS_LAUNCH_CHECK("recon_fast_kernel");
+  return VISS_OK;
+}
+
+__global__ void recon_reduce_kernel(const float2* __restrict__ part, int nsplit, int64_t J, float norm,
+                                    float2* out) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= J) return;
+  float sr = 0.f, si = 0.f;
+  for (int s = 0; s < nsplit; ++s) {
+    const float2 v = part[(int64_t)s * J + j];
+    sr += v.x;
+    si += v.y;
+  }
+  out[j] = make_float2(-sr * norm, -si * norm);
+}
+
+int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, float2* out, cudaStream_t st) {
+  if (J <= 0) return VISS_OK;
+  recon_reduce_kernel<<<(unsigned)((J + 255) / 256), 256, 0, st>>>(partial, nsplit, J, norm, out);
+  VISS_LAUNCH_CHECK("recon_reduce_kernel");
+  return VISS_OK;
+}
+
+// ---------------------------------------------------------------- plain
+// The reference's plain recon, restated: one thread per pixel, FP32 phase
+//   ph = u*l/d + v*m/d + w*(n + n_offset)/d,  x = +2 pi ph   (vissGen10M_shade.cu:169)
+// precise sincosf, register accumulator (optim1, :235-271); reference ratio
+// mask evaluated per term from r1 = M1/M2, r2 = M3/M4 (:166).
+struct PlainRecArgs {
+  const float *u, *v, *w, *wgt, *V, *l, *m, *n;
+  const float* r1;
+  const float* r2;
+  const int32_t* snap;
+  const int32_t* pair;
+  const float* sat_pos;
+  int64_t K, J;
+  int nsat;
+  int rmask;
+  int res;
+  float dl, dm, dn;
+  float noff;
+  float norm;
+  double R;
+  float2* out;
+};
+
+__global__ void recon_plain_kernel(const PlainRecArgs a) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.J) return;
+  const float phiP = floorf((float)(j / a.res));
+  const float thetaP = (float)j - phiP * (float)a.res;
+  const float lj = a.l[j], mj = a.m[j], nj = a.n[j] + a.noff;
+  const float p2 = 2.0f * (float)kPi;
+  float fr = 0.f, fi = 0.f;
+  for (int64_t k = 0; k < a.K; ++k) {
+    if (a.rmask == VISS_RECON_MASK_REF) {
+      const float t0 = a.r1[k], p0 = a.r2[k];
+      if (fabsf(t0 - thetaP) < t0 && fabsf(p0 - phiP) < p0) continue;
+    } else if (a.rmask == VISS_RECON_MASK_GEOMETRIC) {
+      const int s = a.snap[k], pr = a.pair[k];
+      const float* q1 = a.sat_pos + ((int64_t)s * a.nsat + (pr & 0xffff)) * 3;
+      const float* q2 = a.sat_pos + ((int64_t)s * a.nsat + ((pr >> 16) & 0xffff)) * 3;
+      if (geo_occluded_exact(a.l[j], a.m[j], a.n[j], q1, a.R) || geo_occluded_exact(a.l[j], a.m[j], a.n[j], q2, a.R))
+        continue;
+    }
+    const float ph = a.u[k] * lj / a.dl + a.v[k] * mj / a.dm + a.w[k] * nj / a.dn;
+    float sn, cs;
+    sincosf(p2 * ph, &sn, &cs);
+    const float wg = a.wgt ? a.wgt[k] : 1.0f;
+    const float yr = wg * a.V[2 * k], yi = wg * a.V[2 * k + 1];
+    fr += yr * cs - yi * sn;
+    fi += yr * sn + yi * cs;
+  }
+  a.out[j] = make_float2(fr * a.norm, fi * a.norm);
+}
+
+int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
+                       const viss_geometry* geo, const float* V, const float* ratios, const float* dlmn,
+                       float2* out, cudaStream_t st) {
+  PlainRecArgs a{};
+  a.u = vis.u; a.v = vis.v; a.w = vis.w; a.wgt = vis.wgt; a.V = V;
+  a.l = sky.l; a.m = sky.m; a.n = sky.n;
+  a.r1 = ratios; a.r2 = ratios ? ratios + vis.K : nullptr;
+  a.snap = vis.snap; a.pair = vis.pair;
+  a.sat_pos = geo ? geo->sat_pos : nullptr;
+  a.nsat = geo ? geo->nsat : 0;
+  a.K = vis.K; a.J = sky.J;
+  a.rmask = cfg.recon_mask;
+  a.res = cfg.res > 0 ? cfg.res : 1;
+  a.dl = dlmn[0]; a.dm = dlmn[1]; a.dn = dlmn[2];
+  a.noff = (float)cfg.n_offset;
+  a.norm = (float)cfg.norm;
+  a.R = cfg.moon_radius_km;
+  a.out = out;
+  if (a.J <= 0) return VISS_OK;
+  recon_plain_kernel<<<(unsigned)((a.J + 255) / 256), 256, 0, st>>>(a);
+  VISS_LAUNCH_CHECK("recon_plain_kernel");
+  return VISS_OK;
+}
+
+}  // namespace viss

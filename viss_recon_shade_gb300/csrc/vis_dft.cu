@@ -1,0 +1,421 @@
+// vis_dft.cu -- shaded visibility DFT (replaces visscal, vissGen10M_shade.cu:108-145).
+//
+// V_k = sum_j C_kj exp(-2 pi i t_kj),  t_kj = s (u_k l_j + v_k m_j + w_k (n_j + n_offset))
+//
+// Tiled kernel: a CTA owns VIS_ROWS = 1024 visibilities (4 per thread, in
+// registers) and streams the sky through shared memory in tiles of VIS_P
+// pixels; every thread reads each pixel record as a broadcast.  Per term:
+//   3 IMAD (phase mod 1 turn in 32-bit fixed point; exact for integer uvw)
+//   [+3 IMAD.HI +1 LEA for fractional uvw] [+4 FFMA compensation]
+//   1 LOP/LEA + 1 FFMA (turns -> angle), __sincosf (2 SFU ops), 2 FFMA (MAC).
+// The occlusion predicate is evaluated inline per tile:
+//   GEOMETRIC: pixels are classified against a cone bounding the shadow cones
+//     of every satellite used by the CTA's rows -- all visible / all occluded /
+//     mixed -- and compacted into a fast list (brightness or occluded value,
+//     no per-term test) and a mixed list (per-term test against the row's two
+//     satellites, decided in double within GEO_EPS of the limb).
+//   REF_*: per-row window (row range x column range on the fine grid); tiles
+//     no window of the CTA touches run the unmasked loop.
+// Pixel chunks (blockIdx.y) give partial sums, reduced in a fixed order.
+#include "viss_internal.cuh"
+
+namespace viss {
+
+template <bool FRAC, bool COMP>
+__device__ __forceinline__ void vis_term(const int4& a, const int4& b, const float4& lo, float c, int U,
+                                         int V, int W, int FU, int FV, int FW, float UF, float VF, float WF,
+                                         float& ar, float& ai) {
+  uint32_t q = (uint32_t)U * (uint32_t)a.x + (uint32_t)V * (uint32_t)a.y + (uint32_t)W * (uint32_t)a.z +
+               (uint32_t)PHASE_BIAS;
+  if (FRAC) {
+    const uint32_t h = (uint32_t)mulhi(FU, b.x) + (uint32_t)mulhi(FV, b.y) + (uint32_t)mulhi(FW, b.z);
+    q += h << 2;
+  }
+  float x = turns_to_angle(q);
+  if (COMP) {
+    const float d = fmaf(UF, lo.x, fmaf(VF, lo.y, WF * lo.z));
+    x = fmaf(d, K2PI, x);
+  }
+  float sn, cs;
+  __sincosf(x, &sn, &cs);
+  ar = fmaf(c, cs, ar);
+  ai = fmaf(c, sn, ai);
+}
+
+// fast geometric test against one satellite: s_hat . p_hat + cos(alpha) < 0,
+// re-decided exactly near the limb.
+__device__ __forceinline__ bool geo_test(const float4& g, const float4& d, int gidx, const VisParams& p) {
+  const float e = fmaf(g.x, d.x, fmaf(g.y, d.y, fmaf(g.z, d.z, d.w)));
+  if (fabsf(e) >= GEO_EPS) return e < 0.f;
+  const int j = __float_as_int(g.w);
+  return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
+}
+
+// REF window membership of fine pixel (q, r) / index j for window {lo_a, lo_b, M1, M2}.
+__device__ __forceinline__ bool ref_hit(const int4& wv, int q, int r, int64_t j, int res) {
+  if (wv.x > wv.y) return false;
+  if (wv.z + 1 >= 0 && wv.w <= res) return q >= wv.x && q <= wv.y && r > wv.z && r < wv.w;
+  // general: exists lo in [lo_a, lo_b] with lo*res + M1 + 1 <= j < lo*res + M2
+  const int64_t hi_num = j - wv.z - 1, lo_num = j - wv.w + 1;
+  int64_t lo_max = hi_num >= 0 ? hi_num / res : -((-hi_num + res - 1) / res);     // floor
+  int64_t lo_min = lo_num >= 0 ? (lo_num + res - 1) / res : -((-lo_num) / res);   // ceil
+  if (lo_min < wv.x) lo_min = wv.x;
+  if (lo_max > wv.y) lo_max = wv.y;
+  return lo_min <= lo_max;
+}
+
+template <int MASK, bool COMP>
+struct VisSmem {
+  static constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
+  static constexpr bool REF = MASK == VISS_MASK_REF_QUIRK || MASK == VISS_MASK_REF_INTENDED;
+  int4 p0[VIS_P];
+  int4 p1[VIS_P];
+  float4 lo[COMP ? VIS_P : 1];
+  float4 geo[GEO ? VIS_P : 1];
+  int2 qr[REF ? VIS_P : 1];
+  int wcnt[VIS_THREADS / 32][2];
+};
+
+template <int MASK, bool FRAC, bool COMP>
+__device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>& sm) {
+  constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
+  constexpr bool REF = MASK == VISS_MASK_REF_QUIRK || MASK == VISS_MASK_REF_INTENDED;
+  int4* const s_p0 = sm.p0;
+  int4* const s_p1 = sm.p1;
+  float4* const s_lo = sm.lo;
+  float4* const s_geo = sm.geo;
+  int2* const s_qr = sm.qr;
+  auto& s_wcnt = sm.wcnt;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t row0 = (int64_t)blockIdx.x * VIS_ROWS;
+  const int split = blockIdx.y;
+
+  int U[VIS_TK], V[VIS_TK], W[VIS_TK], GM[VIS_TK];
+  int FU[VIS_TK], FV[VIS_TK], FW[VIS_TK], GN[VIS_TK];
+  float UF[VIS_TK], VF[VIS_TK], WF[VIS_TK];
+  int4 WIN[REF ? VIS_TK : 1];
+  float ar[VIS_TK], ai[VIS_TK];
+#pragma unroll
+  for (int i = 0; i < VIS_TK; ++i) {
+    const int64_t k = row0 + tid + i * VIS_THREADS;  // rows are padded to a whole block
+    const int4 r0 = p.rows0[k];
+    U[i] = r0.x; V[i] = r0.y; W[i] = r0.z; GM[i] = r0.w;
+    FU[i] = FV[i] = FW[i] = 0; GN[i] = 0;
+    if (FRAC || GEO) {
+      const int4 r1 = p.rows1[k];
+      FU[i] = r1.x; FV[i] = r1.y; FW[i] = r1.z; GN[i] = r1.w;
+    }
+    UF[i] = VF[i] = WF[i] = 0.f;
+    if (COMP) {
+      const float4 f = p.rowsf[k];
+      UF[i] = f.x; VF[i] = f.y; WF[i] = f.z;
+    }
+    if (REF) WIN[i] = p.win[k];
+    ar[i] = 0.f; ai[i] = 0.f;
+  }
+  float4 cone0 = make_float4(0.f, 0.f, 0.f, 2.f), cone1 = make_float4(-2.f, 0.f, 0.f, 0.f);
+  if (GEO) {
+    cone0 = p.cones[2 * blockIdx.x];
+    cone1 = p.cones[2 * blockIdx.x + 1];
+  }
+  const float occ_val = p.occ_val;
+
+  const int64_t jb = (int64_t)split * p.jchunk;
+  int64_t je = jb + p.jchunk;
+  if (je > p.J) je = p.J;
+
+  for (int64_t tile = jb; tile < je; tile += VIS_P) {
+    const int np = (int)((je - tile) < VIS_P ? (je - tile) : VIS_P);
+    __syncthreads();  // previous tile fully consumed
+    int nfast = np, nmix = 0;
+    bool masked_tile = false;
+    if (GEO) {
+      constexpr int Q = VIS_P / VIS_THREADS;
+      bool isF[Q], isM[Q];
+      int4 a[Q], b[Q];
+      float4 lo[Q], g[Q];
+#pragma unroll
+      for (int qq = 0; qq < Q; ++qq) {
+        const int i = tid + qq * VIS_THREADS;
+        isF[qq] = isM[qq] = false;
+        if (i < np) {
+          const int64_t j = tile + i;
+          a[qq] = p.pix0[j];
+          if (FRAC) b[qq] = p.pix1[j];
+          if (COMP) lo[qq] = p.plo[j];
+          g[qq] = p.pgeo[j];
+          const float d = fmaf(g[qq].x, cone0.x, fmaf(g[qq].y, cone0.y, g[qq].z * cone0.z));
+          if (d > cone0.w) {  // occluded for every row of the block
+            a[qq].w = __float_as_int(occ_val);
+            isF[qq] = occ_val != 0.f;
+          } else if (d < cone1.x) {  // visible for every row
+            isF[qq] = true;
+          } else {
+            isM[qq] = true;
+          }
+        }
+      }
+      unsigned bF[Q], bM[Q];
+      int cf = 0, cm = 0;
+#pragma unroll
+      for (int qq = 0; qq < Q; ++qq) {
+        bF[qq] = __ballot_sync(0xffffffffu, isF[qq]);
+        bM[qq] = __ballot_sync(0xffffffffu, isM[qq]);
+        cf += __popc(bF[qq]);
+        cm += __popc(bM[qq]);
+      }
+      if (lane == 0) { s_wcnt[warp][0] = cf; s_wcnt[warp][1] = cm; }
+      __syncthreads();
+      int offF = 0, offM = 0, totF = 0, totM = 0;
+#pragma unroll
+      for (int w2 = 0; w2 < VIS_THREADS / 32; ++w2) {
+        const int f = s_wcnt[w2][0], m = s_wcnt[w2][1];
+        if (w2 < warp) { offF += f; offM += m; }
+        totF += f; totM += m;
+      }
+      const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+      for (int qq = 0; qq < Q; ++qq) {
+        if (isF[qq]) {
+          const int pos = offF + __popc(bF[qq] & lt);
+          s_p0[pos] = a[qq];
+          if (FRAC) s_p1[pos] = b[qq];
+          if (COMP) s_lo[pos] = lo[qq];
+        }
+        if (isM[qq]) {
+          const int pos = VIS_P - 1 - (offM + __popc(bM[qq] & lt));
+          s_p0[pos] = a[qq];
+          if (FRAC) s_p1[pos] = b[qq];
+          if (COMP) s_lo[pos] = lo[qq];
+          s_geo[pos] = g[qq];
+        }
+        offF += __popc(bF[qq]);
+        offM += __popc(bM[qq]);
+      }
+      nfast = totF;
+      nmix = totM;
+      __syncthreads();
+    } else {
+      for (int i = tid; i < np; i += VIS_THREADS) {
+        const int64_t j = tile + i;
+        s_p0[i] = p.pix0[j];
+        if (FRAC) s_p1[i] = p.pix1[j];
+        if (COMP) s_lo[i] = p.plo[j];
+        if (REF) s_qr[i] = p.pqr[j];
+      }
+      bool hit = false;
+      if (REF) {
+        // bounding fine-index range of each window against [tile, tile + np)
+#pragma unroll
+        for (int i = 0; i < VIS_TK; ++i) {
+          const int4 wv = WIN[i];
+          if (wv.x <= wv.y && wv.z + 1 < wv.w) {
+            const int64_t lo_idx = (int64_t)wv.x * p.res + wv.z + 1;
+            const int64_t hi_idx = (int64_t)wv.y * p.res + wv.w - 1;
+            if (lo_idx < tile + np && hi_idx >= tile) hit = true;
+          }
+        }
+      }
+      masked_tile = __syncthreads_or(hit) != 0;
+    }
+
+    if (!masked_tile) {
+#pragma unroll 2
+      for (int pi = 0; pi < nfast; ++pi) {
+        const int4 a = s_p0[pi];
+        int4 b = make_int4(0, 0, 0, 0);
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FRAC) b = s_p1[pi];
+        if (COMP) lo = s_lo[pi];
+        const float c = __int_as_float(a.w);
+#pragma unroll
+        for (int i = 0; i < VIS_TK; ++i)
+          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+                               ar[i], ai[i]);
+      }
+    } else if (REF) {
+      for (int pi = 0; pi < np; ++pi) {
+        const int4 a = s_p0[pi];
+        int4 b = make_int4(0, 0, 0, 0);
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FRAC) b = s_p1[pi];
+        if (COMP) lo = s_lo[pi];
+        const int2 qr = s_qr[pi];
+        const float c0 = __int_as_float(a.w);
+#pragma unroll
+        for (int i = 0; i < VIS_TK; ++i) {
+          const float c = ref_hit(WIN[i], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
+          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+                               ar[i], ai[i]);
+        }
+      }
+    }
+    if (GEO) {
+      for (int mi = 0; mi < nmix; ++mi) {
+        const int pi = VIS_P - 1 - mi;
+        const int4 a = s_p0[pi];
+        int4 b = make_int4(0, 0, 0, 0);
+        float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (FRAC) b = s_p1[pi];
+        if (COMP) lo = s_lo[pi];
+        const float4 g = s_geo[pi];
+        const float c0 = __int_as_float(a.w);
+#pragma unroll
+        for (int i = 0; i < VIS_TK; ++i) {
+          const float4 dm = __ldg(p.satdir + GM[i]);
+          const float4 dn = __ldg(p.satdir + GN[i]);
+          const bool occ = geo_test(g, dm, GM[i], p) || geo_test(g, dn, GN[i], p);
+          const float c = occ ? occ_val : c0;
+          if (c != 0.f)
+            vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+                                 ar[i], ai[i]);
+        }
+      }
+    }
+  }
+
+  // V = -ar + i ai  (the angle carried an extra half turn)
+#pragma unroll
+  for (int i = 0; i < VIS_TK; ++i) {
+    const int64_t k = row0 + tid + i * VIS_THREADS;
+    if (k < p.K) {
+      if (p.nsplit == 1) p.out[k] = make_float2(-ar[i], ai[i]);
+      else p.out[(int64_t)split * p.K + k] = make_float2(ar[i], ai[i]);
+    }
+  }
+}
+
+// Integer-valued uvw (the reference's ceil(), MIncline:156-158) need no
+// fractional term; the row prep sets flags[0] when any uvw is fractional and
+// the kernel picks its loop from that flag (uniform branch, no host sync).
+template <int MASK, bool COMP>
+__global__ void __launch_bounds__(VIS_THREADS, 3) vis_fast_kernel(const VisParams p) {
+  __shared__ VisSmem<MASK, COMP> sm;
+  if (__ldg(p.flags) != 0) vis_body<MASK, true, COMP>(p, sm);
+  else vis_body<MASK, false, COMP>(p, sm);
+}
+
+template <int MASK>
+static void launch_mask(const VisParams& p, dim3 grid, bool comp, cudaStream_t st) {
+  if (comp) vis_fast_kernel<MASK, true><<<grid, VIS_THREADS, 0, st>>>(p);
+  else vis_fast_kernel<MASK, false><<<grid, VIS_THREADS, 0, st>>>(p);
+}
+
+int launch_vis_fast(const VisParams& p, int64_t nrb, bool comp, cudaStream_t st) {
+  const dim3 grid((unsigned)nrb, (unsigned)p.nsplit);
+  switch (p.mask) {
+    case VISS_MASK_NONE: launch_mask<VISS_MASK_NONE>(p, grid, comp, st); break;
+    case VISS_MASK_REF_QUIRK: launch_mask<VISS_MASK_REF_QUIRK>(p, grid, comp, st); break;
+    case VISS_MASK_REF_INTENDED: launch_mask<VISS_MASK_REF_INTENDED>(p, grid, comp, st); break;
+    case VISS_MASK_GEOMETRIC: launch_mask<VISS_MASK_GEOMETRIC>(p, grid, comp, st); break;
+    default: return fail(VISS_ERR_INVALID, "unknown mask mode");
+  }
+  VISS_LAUNCH_CHECK("vis_fast_kernel");
+  return VISS_OK;
+}
+
+__global__ void vis_reduce_kernel(const float2* __restrict__ part, int nsplit, int64_t K, float2* out) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  float sr = 0.f, si = 0.f;
+  for (int s = 0; s < nsplit; ++s) {
+    const float2 v = part[(int64_t)s * K + k];
+    sr += v.x;
+    si += v.y;
+  }
+  out[k] = make_float2(-sr, si);
+}
+
+int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st) {
+  if (K <= 0) return VISS_OK;
+  vis_reduce_kernel<<<(unsigned)((K + 255) / 256), 256, 0, st>>>(partial, nsplit, K, out);
+  VISS_LAUNCH_CHECK("vis_reduce_kernel");
+  return VISS_OK;
+}
+
+// ---------------------------------------------------------------- plain
+// The reference's plain method, restated: one thread per visibility, the sky
+// read from global memory, FP32 phase
+//   ph = u*l/d + v*m/d + w*(n-1)/d,  x = -2 pi ph  (vissGen10M_shade.cu:137-138)
+// with precise sincosf, accumulated in registers (optim1, :154-205), times the
+// trailing exp(-2 pi i (1 + n_offset) w / d) (:143).  Masks as in the tiled kernel.
+struct PlainVisArgs {
+  const float *u, *v, *w, *l, *m, *n, *bright;
+  const int32_t* shade;
+  const int32_t* snap;
+  const int32_t* pair;
+  const float* sat_pos;
+  int64_t K, J;
+  int nsat;
+  int mask;
+  int res;
+  int trunc;
+  float occ;
+  float dl, dm, dn;
+  float trail;  // 1 + n_offset
+  double R;
+  float2* out;
+};
+
+__device__ bool plain_geo(const PlainVisArgs& a, int64_t k, int64_t j) {
+  const int s = a.snap[k], pr = a.pair[k];
+  const float* p1 = a.sat_pos + ((int64_t)s * a.nsat + (pr & 0xffff)) * 3;
+  const float* p2 = a.sat_pos + ((int64_t)s * a.nsat + ((pr >> 16) & 0xffff)) * 3;
+  return geo_occluded_exact(a.l[j], a.m[j], a.n[j], p1, a.R) || geo_occluded_exact(a.l[j], a.m[j], a.n[j], p2, a.R);
+}
+
+__global__ void vis_plain_kernel(const PlainVisArgs a) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const float uk = a.u[k], vk = a.v[k], wk = a.w[k];
+  int4 wv = make_int4(1, 0, 0, 0);
+  if ((a.mask == VISS_MASK_REF_QUIRK || a.mask == VISS_MASK_REF_INTENDED) && a.shade) {
+    const int M1 = a.shade[4 * k], M2 = a.shade[4 * k + 1], M3 = a.shade[4 * k + 2], M4 = a.shade[4 * k + 3];
+    if (a.mask == VISS_MASK_REF_QUIRK) { if (M3 <= 0 && M4 >= 0) wv = make_int4(0, M4, M1, M2); }
+    else if (M3 <= M4) wv = make_int4(M3, M4, M1, M2);
+  }
+  const float m2pi = -2.0f * (float)kPi;
+  float ar = 0.f, ai = 0.f;
+  for (int64_t j = 0; j < a.J; ++j) {
+    float c = a.bright[j];
+    if (a.trunc) c = (float)(int)c;
+    if (wv.x <= wv.y) {
+      const int64_t q = j / a.res, r = j % a.res;
+      if (ref_hit(wv, (int)q, (int)r, j, a.res)) c = a.occ;
+    } else if (a.mask == VISS_MASK_GEOMETRIC && plain_geo(a, k, j)) {
+      c = a.occ;
+    }
+    const float ph = uk * a.l[j] / a.dl + vk * a.m[j] / a.dm + wk * (a.n[j] - 1.0f) / a.dn;
+    float sn, cs;
+    sincosf(m2pi * ph, &sn, &cs);
+    ar = fmaf(c, cs, ar);
+    ai = fmaf(c, sn, ai);
+  }
+  float sn, cs;
+  sincosf(m2pi * (a.trail * wk / a.dn), &sn, &cs);
+  a.out[k] = make_float2(ar * cs - ai * sn, ar * sn + ai * cs);
+}
+
+int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
+                     const viss_geometry* geo, const float* dlmn, float2* out, cudaStream_t st) {
+  PlainVisArgs a{};
+  a.u = vis.u; a.v = vis.v; a.w = vis.w;
+  a.l = sky.l; a.m = sky.m; a.n = sky.n; a.bright = sky.bright;
+  a.shade = vis.shade; a.snap = vis.snap; a.pair = vis.pair;
+  a.sat_pos = geo ? geo->sat_pos : nullptr;
+  a.nsat = geo ? geo->nsat : 0;
+  a.K = vis.K; a.J = sky.J;
+  a.mask = cfg.mask_mode; a.res = cfg.res > 0 ? cfg.res : 1; a.trunc = cfg.trunc_brightness;
+  a.occ = cfg.occluded_value;
+  a.dl = dlmn[0]; a.dm = dlmn[1]; a.dn = dlmn[2];
+  a.trail = (float)(1.0 + cfg.n_offset);
+  a.R = cfg.moon_radius_km;
+  a.out = out;
+  if (a.K <= 0) return VISS_OK;
+  vis_plain_kernel<<<(unsigned)((a.K + 255) / 256), 256, 0, st>>>(a);
+  VISS_LAUNCH_CHECK("vis_plain_kernel");
+  return VISS_OK;
+}
+
+}  // namespace viss
