@@ -206,6 +206,23 @@ VISS_API int viss_shade_windows(const float* u, const float* v, const float* w, 
 /* shadeM normalisation on load (vissGen10M_shade.cu:383-399): (min-1, max-1) per pair. */
 VISS_API int viss_normalise_shade(const int32_t* raw, int64_t K, int32_t* M, void* stream);
 
+/* ------------------------------------------------------------- text files */
+/* The reference's whitespace-separated text files (HOST buffers).  Reading is
+ * chunk-parallel and stops at the first token that does not parse, as the
+ * reference's `while (file >> ...)` loops do; writing formats every value as
+ * std::ostream formats a float by default ("%g", 6 significant digits).
+ *   l.txt / FF.txt carry a count header (vissGen10M_shade.cu:237-238): header = 1.
+ *   uvw files: 3 columns (u v w, MIncline:425) or 4 (u v w freq, vissGen10M_shade.cu:359).
+ *   shadeM files: 4 integer columns (shade1M.cu:118-121).
+ * viss_text_read_floats stores column c of row r at out[c*cap + r]; with out == NULL it only
+ * counts rows.  viss_text_write_floats reads column c of row r at cols[c*stride + r]. */
+VISS_API int viss_text_read_floats(const char* path, int header, int ncols, float* out, int64_t cap,
+                                   int64_t* nrows, int64_t* header_value);
+VISS_API int viss_text_read_ints(const char* path, int ncols, int32_t* out, int64_t cap, int64_t* nrows);
+VISS_API int viss_text_write_floats(const char* path, int ncols, const float* cols, int64_t stride,
+                                    int64_t nrows);
+VISS_API int viss_text_write_ints(const char* path, int ncols, const int32_t* rows, int64_t nrows);
+
 /* ------------------------------------------------------------- measurement */
 /* SFU throughput probe (no counterpart in the reference): launches
  * blocks_per_sm * SMs blocks of 256 threads, each thread running `iters` rounds of

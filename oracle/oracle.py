@@ -141,18 +141,18 @@ def recon(cfg: DftCfg, u, v, w, wgt, V, l, m, n, shade=None, geo=None, nthreads=
     return out[:, 0] + 1j * out[:, 1]
 
 
-def vis_plain_f32(cfg: DftCfg, u, v, w, l, m, n, FF, d=2.0, shade=None, nthreads=0):
+def vis_plain_f32(cfg: DftCfg, u, v, w, l, m, n, FF, d=2.0, shade=None, nthreads=0, optim=False):
     u, v, w, l, m, n, FF = map(_f32, (u, v, w, l, m, n, FF))
     shade = _i32(shade)
     K, J = u.size, l.size
     out = np.zeros((K, 2), np.float32)
     lib().oracle_vis_plain_f32(C.byref(cfg), _p(u), _p(v), _p(w), C.c_int64(K), _p(shade), _p(l),
                                _p(m), _p(n), _p(FF), C.c_int64(J), C.c_float(d), _p(out),
-                               C.c_int(nthreads))
+                               C.c_int(nthreads), C.c_int(int(optim)))
     return out[:, 0] + 1j * out[:, 1]
 
 
-def recon_plain_f32(cfg: DftCfg, u, v, w, wgt, V, l, m, n, d=2.0, shade=None, nthreads=0):
+def recon_plain_f32(cfg: DftCfg, u, v, w, wgt, V, l, m, n, d=2.0, shade=None, nthreads=0, optim=False):
     u, v, w, wgt, l, m, n = map(_f32, (u, v, w, wgt, l, m, n))
     Vf = np.ascontiguousarray(np.stack([np.real(V), np.imag(V)], -1), dtype=np.float32)
     shade = _i32(shade)
@@ -160,7 +160,7 @@ def recon_plain_f32(cfg: DftCfg, u, v, w, wgt, V, l, m, n, d=2.0, shade=None, nt
     out = np.zeros((J, 2), np.float32)
     lib().oracle_recon_plain_f32(C.byref(cfg), _p(u), _p(v), _p(w), _p(wgt), _p(Vf), C.c_int64(K),
                                  _p(shade), _p(l), _p(m), _p(n), C.c_int64(J), C.c_float(d), _p(out),
-                                 C.c_int(nthreads))
+                                 C.c_int(nthreads), C.c_int(int(optim)))
     return out[:, 0] + 1j * out[:, 1]
 
 

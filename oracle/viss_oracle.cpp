@@ -312,7 +312,7 @@ ORACLE_API int oracle_recon(const oracle_dft_cfg* cfg, const float* u, const flo
 ORACLE_API int oracle_vis_plain_f32(const oracle_dft_cfg* cfg, const float* u, const float* v,
                                     const float* w, int64_t K, const int32_t* shade, const float* l,
                                     const float* m, const float* n, const float* FF, int64_t J,
-                                    float d, float* V, int nthreads) {
+                                    float d, float* V, int nthreads, int optim) {
   const float two_pi_f = -2.0f * (float)kPi;  // (0 - i) * 2 * pi, imaginary part
 #pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
   for (int64_t k = 0; k < K; ++k) {
@@ -323,7 +323,10 @@ ORACLE_API int oracle_vis_plain_f32(const oracle_dft_cfg* cfg, const float* u, c
         const int32_t* M = shade + 4 * k;
         if (ref_window_hit_fast(j, cfg->res, M[0], M[1], M[2], M[3], cfg->mask_mode)) c = cfg->occluded_value;
       }
-      const float ph = u[k] * l[j] / d + v[k] * m[j] / d + w[k] * (n[j] - 1.0f) / d;
+      // plain: u*l/dl + ... (:137); optim: u/dl hoisted, sum contracted to FMAs
+      // (vissGen10M_shade_optim1.cu:161-163, 193)
+      const float ph = optim ? std::fmaf(w[k] * (1.0f / d), n[j] - 1.0f, std::fmaf(v[k] * (1.0f / d), m[j], (u[k] * (1.0f / d)) * l[j]))
+                             : u[k] * l[j] / d + v[k] * m[j] / d + w[k] * (n[j] - 1.0f) / d;
       const float x = two_pi_f * ph;
       ar = ar + c * cosf(x);
       ai = ai + c * sinf(x);
@@ -339,7 +342,7 @@ ORACLE_API int oracle_vis_plain_f32(const oracle_dft_cfg* cfg, const float* u, c
 ORACLE_API int oracle_recon_plain_f32(const oracle_dft_cfg* cfg, const float* u, const float* v,
                                       const float* w, const float* wgt, const float* Vin, int64_t K,
                                       const int32_t* shade, const float* l, const float* m,
-                                      const float* n, int64_t J, float d, float* F, int nthreads) {
+                                      const float* n, int64_t J, float d, float* F, int nthreads, int optim) {
   const float two_pi_f = 2.0f * (float)kPi;
   std::vector<float> r1(K, 0.f), r2(K, 0.f);
   if (shade) {
@@ -355,7 +358,8 @@ ORACLE_API int oracle_recon_plain_f32(const oracle_dft_cfg* cfg, const float* u,
     float fr = 0.f, fi = 0.f;
     for (int64_t k = 0; k < K; ++k) {
       if (shade && std::fabs(r1[k] - thetaP) < r1[k] && std::fabs(r2[k] - phiP) < r2[k]) continue;
-      const float ph = u[k] * l[j] / d + v[k] * m[j] / d + w[k] * n[j] / d;
+      const float ph = optim ? std::fmaf(w[k], n[j] * (1.0f / d), std::fmaf(v[k], m[j] * (1.0f / d), u[k] * (l[j] * (1.0f / d))))
+                             : u[k] * l[j] / d + v[k] * m[j] / d + w[k] * n[j] / d;
       const float x = two_pi_f * ph;
       const float cs = cosf(x), sn = sinf(x);
       const float yr = wgt[k] * Vin[2 * k], yi = wgt[k] * Vin[2 * k + 1];
@@ -414,8 +418,9 @@ namespace {
 
 // Window of uvwPosition (:113-151): snapshot g of satellite `sat` reads global
 // sample `circle` of the satellite's (OrbitCounts*OrbitRes) array.  Returns
-// 0 normally, 1 when the reference zero-fills, 2 when circle == total (the
-// reference then reads the next satellite's first sample).
+// 0 normally, 1 when the reference zero-fills, 2 when circle == total: the
+// reference then reads x[(sat+1)*total], the next satellite's slot, which its
+// loop (:224-308) has not filled yet -- the zero of the initialised vector.
 inline int window_index(int64_t g, int orbit_res, int orbit_counts, int64_t* circle) {
   const int span = orbit_res / 3;
   const int interval = orbit_res / 360 * 10;
@@ -523,20 +528,17 @@ ORACLE_API int oracle_orbit_positions(const oracle_orbit_cfg* cfg, int mode, flo
     const int kind = window_index(g, cfg->orbit_res, cfg->orbit_counts, &circle);
     for (int sat = 0; sat < cfg->nsat; ++sat) {
       float* o = pos + (g * cfg->nsat + sat) * 3;
-      int src_sat = sat;
-      int64_t src = circle;
-      if (kind == 1 || (kind == 2 && sat + 1 >= cfg->nsat)) {
+      if (kind != 0) {
         o[0] = o[1] = o[2] = 0.f;
         continue;
       }
-      if (kind == 2) { src_sat = sat + 1; src = 0; }
       (void)total;
       if (mode == 0) {
         double p[3];
-        orbit_position_f64(cfg, src_sat, src, p);
+        orbit_position_f64(cfg, sat, circle, p);
         o[0] = (float)p[0]; o[1] = (float)p[1]; o[2] = (float)p[2];
       } else {
-        orbit_position_f32(cfg, src_sat, src, o);
+        orbit_position_f32(cfg, sat, circle, o);
       }
     }
   }
@@ -553,9 +555,8 @@ ORACLE_API int oracle_orbit_positions_f64(const oracle_orbit_cfg* cfg, double* p
     const int kind = window_index(g, cfg->orbit_res, cfg->orbit_counts, &circle);
     for (int sat = 0; sat < cfg->nsat; ++sat) {
       double* o = pos + (g * cfg->nsat + sat) * 3;
-      if (kind == 1 || (kind == 2 && sat + 1 >= cfg->nsat)) { o[0] = o[1] = o[2] = 0.0; continue; }
-      if (kind == 2) orbit_position_f64(cfg, sat + 1, 0, o);
-      else orbit_position_f64(cfg, sat, circle, o);
+      if (kind != 0) { o[0] = o[1] = o[2] = 0.0; continue; }
+      orbit_position_f64(cfg, sat, circle, o);
     }
   }
   return 0;

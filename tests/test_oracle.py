@@ -127,11 +127,11 @@ def test_window_index_quirks(oracle):
     cfg = oracle.make_orbit_cfg(8, 360, 30, r1_m=r1, r2_m=r2)
     pos = oracle.orbit_positions(cfg, mode=1)
     zero = np.all(pos == 0, axis=2)
-    assert zero[:, 7].sum() == 50 and zero[:, 0].sum() == 49
-    # satellite 0 at the one-past-the-end sample reads satellite 1's first sample
-    p1 = oracle.orbit_positions(oracle.make_orbit_cfg(8, 360, 30, r1_m=r1, r2_m=r2), mode=1)
-    g = np.nonzero(~zero[:, 0] & zero[:, 7])[0]
-    assert g.size == 1 and np.all(p1[g[0], 0] != 0)
+    # 49 zero-filled samples plus the one-past-the-end read, which lands in the
+    # next satellite's slot before the reference has computed it: zero as well
+    assert np.all(zero.sum(0) == 50)
+    cfg40 = oracle.make_orbit_cfg(8, 360, 40, r1_m=r1, r2_m=r2)
+    assert not np.all(oracle.orbit_positions(cfg40, mode=1) == 0, axis=2).any()
 
 
 def test_orbit_fp32_mimic_close_to_fp64(oracle):

@@ -83,6 +83,11 @@ _SIGS = {
                                      C.c_size_t, _P]),
     "viss_normalise_shade": (C.c_int, [_P, C.c_int64, _P, _P]),
     "viss_sfu_probe": (C.c_int, [C.c_int, C.c_int, _P, C.POINTER(C.c_int64), _P]),
+    "viss_text_read_floats": (C.c_int, [C.c_char_p, C.c_int, C.c_int, _P, C.c_int64, C.POINTER(C.c_int64),
+                                        C.POINTER(C.c_int64)]),
+    "viss_text_read_ints": (C.c_int, [C.c_char_p, C.c_int, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "viss_text_write_floats": (C.c_int, [C.c_char_p, C.c_int, _P, C.c_int64, C.c_int64]),
+    "viss_text_write_ints": (C.c_int, [C.c_char_p, C.c_int, _P, C.c_int64]),
 }
 
 
@@ -96,7 +101,7 @@ def declared_symbols() -> list[str]:
 def _load():
     if not LIB_PATH.exists():
         raise ImportError(
-            f"libvissgb.so not built ({LIB_PATH}); run `python -m viss_recon_shade_gb300.build` "
+            f"libvissgb.so not built ({LIB_PATH}); run `python viss_recon_shade_gb300/build.py` "
             "or __graft_entry__.build() -- there is no CPU fallback")
     lib = C.CDLL(str(LIB_PATH))
     for name, (res, args) in _SIGS.items():

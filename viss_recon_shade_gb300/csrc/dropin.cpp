@@ -1,0 +1,389 @@
+// dropin.cpp -- drop-in replacements for the reference's programs, driving
+// libvissgb.so through its C ABI with the reference's directory layout and
+// text formats.  One binary; the program is chosen by the name it is run as
+// (bin/ holds links) or by the first argument:
+//
+//   vissGen10M_shade   vissGen10M_shade.cu:178-611 (+ _optim1/_optim2 file names)
+//   vissGen1M_shade    vissGen1M_shade_optim1.cu:265-726 (uvwMap130 weights, NX expansion)
+//   shade1M/10M/30M    shade1M.cu:130-280, shade10M.cu, shade30M.cu
+//   MIncline_generate_uvw_float   MIncline_generate_uvw_float.cu:184-484
+//
+// Every constant the reference hard-codes is a flag with the reference's value
+// as default.  Non-identity fine->coarse sky maps are rejected (VISS_ERR_UNSUPPORTED).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <sys/stat.h>
+#include <unordered_map>
+#include <vector>
+
+#include "viss_gb300.h"
+
+namespace {
+
+struct Args {
+  std::map<std::string, std::string> kv;
+  std::string get(const std::string& k, const std::string& d) const {
+    auto it = kv.find(k);
+    return it == kv.end() ? d : it->second;
+  }
+  long geti(const std::string& k, long d) const { return std::stol(get(k, std::to_string(d))); }
+  double getd(const std::string& k, double d) const { return std::stod(get(k, std::to_string(d))); }
+};
+
+Args parse(int argc, char** argv, int first) {
+  Args a;
+  for (int i = first; i < argc; ++i) {
+    std::string s = argv[i];
+    if (s.rfind("--", 0) == 0) {
+      auto eq = s.find('=');
+      if (eq != std::string::npos) a.kv[s.substr(2, eq - 2)] = s.substr(eq + 1);
+      else if (i + 1 < argc && std::string(argv[i + 1]).rfind("--", 0) != 0) a.kv[s.substr(2)] = argv[++i];
+      else a.kv[s.substr(2)] = "1";
+    }
+  }
+  return a;
+}
+
+#define CHECKV(call)                                                                       \
+  do {                                                                                     \
+    int rc_ = (call);                                                                      \
+    if (rc_ != VISS_OK) {                                                                  \
+      std::fprintf(stderr, "%s failed: %s (%s)\n", #call, viss_status_str(rc_), viss_last_error()); \
+      return 1;                                                                            \
+    }                                                                                      \
+  } while (0)
+
+#define CHECKC(call)                                                                       \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      std::fprintf(stderr, "%s failed: %s\n", #call, cudaGetErrorString(e_));              \
+      return 1;                                                                            \
+    }                                                                                      \
+  } while (0)
+
+template <class T>
+struct Dev {
+  T* p = nullptr;
+  size_t n = 0;
+  ~Dev() { if (p) cudaFree(p); }
+  int alloc(size_t count) {
+    n = count;
+    return cudaMalloc(&p, sizeof(T) * (count ? count : 1)) == cudaSuccess ? 0 : 1;
+  }
+  int up(const T* h, size_t count) {
+    if (alloc(count)) return 1;
+    return count && cudaMemcpy(p, h, sizeof(T) * count, cudaMemcpyHostToDevice) != cudaSuccess;
+  }
+};
+
+double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void mkdir_p(const std::string& d) { ::mkdir(d.c_str(), 0755); }
+
+int read_col(const std::string& path, bool header, std::vector<float>& out, int64_t* hv = nullptr) {
+  int64_t rows = 0, h = 0;
+  int rc = viss_text_read_floats(path.c_str(), header, 1, nullptr, 0, &rows, &h);
+  if (rc) return rc;
+  if (header && hv) *hv = h;
+  out.resize(rows);
+  return viss_text_read_floats(path.c_str(), header, 1, out.data(), rows, &rows, &h);
+}
+
+int read_cols(const std::string& path, int ncols, std::vector<float>& out, int64_t* rows) {
+  int rc = viss_text_read_floats(path.c_str(), 0, ncols, nullptr, 0, rows, nullptr);
+  if (rc) return rc;
+  out.resize((size_t)*rows * ncols);
+  return viss_text_read_floats(path.c_str(), 0, ncols, out.data(), *rows, rows, nullptr);
+}
+
+// ------------------------------------------------------------------ vissGen
+// Shared by the 10M and 1M programs: per period, read uvw (+weights) and
+// shadeM, run the vis DFT and the reconstruction, write Re(F).
+int vissgen(const Args& a, bool tenM) {
+  const std::string root = a.get("root", ".");
+  const int RES = (int)a.geti("res", tenM ? 20940 : 2094);
+  const std::string variant = a.get("variant", tenM ? "plain" : "optim1");
+  const int start_period = (int)a.geti("start-period", tenM && variant == "optim2" ? 1 : 0);
+  const int days = (int)a.geti("days", tenM && variant == "optim2" ? 34 : 1);
+  const std::string prec_s = a.get("precision", "fast");
+  const int precision = prec_s == "plain" ? VISS_PREC_PLAIN : prec_s == "comp" ? VISS_PREC_COMPENSATED : VISS_PREC_FAST;
+  const std::string mask_s = a.get("mask", "quirk");
+  const int mask = mask_s == "none" ? VISS_MASK_NONE : mask_s == "intended" ? VISS_MASK_REF_INTENDED : VISS_MASK_REF_QUIRK;
+  const float d = (float)(2 * RES / (RES - 1));  // integer division, vissGen10M_shade.cu:183-185
+  const std::string lmn = tenM ? root + "/lmn10M/" : root + "/frequency_1M/";
+  const std::string freq_dir = tenM ? root + "/frequency_10M/" : root + "/frequency_1M/";
+  const std::string dur = tenM ? "frequency10M" : "frequency1M";
+
+  std::vector<float> l, m, n, C, NX, FF, NXq;
+  int64_t J = 0, X = 0;
+  if (read_col(lmn + "l.txt", true, l, &J) || read_col(lmn + "m.txt", false, m) || read_col(lmn + "n.txt", false, n) ||
+      read_col(lmn + "C.txt", false, C) || read_col(lmn + "NX.txt", false, NX) || read_col(lmn + "FF.txt", true, FF, &X)) {
+    std::fprintf(stderr, "cannot read the sky files under %s: %s\n", lmn.c_str(), viss_last_error());
+    return 1;
+  }
+  if ((int64_t)l.size() < J || (int64_t)m.size() < J || (int64_t)n.size() < J || (int64_t)FF.size() < X) {
+    std::fprintf(stderr, "sky files shorter than their headers\n");
+    return 1;
+  }
+  l.resize(J); m.resize(J); n.resize(J); FF.resize(X); NX.resize(std::min<size_t>(NX.size(), (size_t)X));
+  // identity fine->coarse map only
+  bool identity = X == J && (int64_t)NX.size() == X;
+  for (int64_t i = 0; identity && i < X; ++i) identity = (int64_t)NX[i] == i + 1;
+  if (tenM) {
+    std::vector<float> cl;
+    if (read_col(lmn + "countLoc.txt", false, cl) == VISS_OK && read_col(lmn + "NXq.txt", false, NXq) == VISS_OK) {
+      for (int64_t j = 0; identity && j < J && j < (int64_t)cl.size(); ++j) identity = cl[j] == 1.0f;
+      for (int64_t i = 0; identity && i < X && i < (int64_t)NXq.size(); ++i) identity = (int64_t)NXq[i] == i;
+    }
+  }
+  if (!identity) {
+    std::fprintf(stderr, "non-identity fine->coarse sky map (NX/countLoc/NXq) is not supported\n");
+    return 2;
+  }
+  for (auto& x : n) x = std::fmax(-1.0f, std::fmin(1.0f, x));  // clip_functor (:308)
+
+  std::unordered_map<long long, float> uvwmap;  // 1M: uvwMap130.txt weights
+  if (!tenM) {
+    std::vector<float> mp;
+    int64_t rows = 0;
+    // header line = count, then "u v w count"
+    if (viss_text_read_floats((freq_dir + "uvwMap130.txt").c_str(), 1, 4, nullptr, 0, &rows, nullptr) == VISS_OK) {
+      mp.resize((size_t)rows * 4);
+      int64_t hv;
+      viss_text_read_floats((freq_dir + "uvwMap130.txt").c_str(), 1, 4, mp.data(), rows, &rows, &hv);
+      for (int64_t r = 0; r < rows; ++r) {
+        const long long key = ((long long)(int)mp[r] * 1000003LL + (long long)(int)mp[rows + r]) * 1000003LL +
+                              (long long)(int)mp[2 * rows + r];
+        uvwmap[key] = mp[3 * rows + r];
+      }
+    }
+  }
+
+  Dev<float> dl_, dm_, dn_, dFF;
+  if (dl_.up(l.data(), J) || dm_.up(m.data(), J) || dn_.up(n.data(), J) || dFF.up(FF.data(), J)) {
+    std::fprintf(stderr, "device allocation failed\n");
+    return 1;
+  }
+  const std::string outdir = tenM ? root + "/F_recon_10M/" : root + "/F_recon_1M/";
+  mkdir_p(outdir);
+  for (int p = start_period; p < days; ++p) {
+    const double t0 = now();
+    std::vector<float> uvw;
+    int64_t K = 0;
+    const std::string uvw_path = freq_dir + (tenM ? "updated_uvw" : "uvw") + std::to_string(p + 1) + dur + ".txt";
+    if (read_cols(uvw_path, tenM ? 4 : 3, uvw, &K)) {
+      std::fprintf(stderr, "cannot read %s\n", uvw_path.c_str());
+      return 1;
+    }
+    std::vector<float> wgt(K, 1.0f);
+    for (int64_t k = 0; k < K; ++k) {
+      if (tenM) {
+        wgt[k] = 1.0f / uvw[3 * K + k];  // uvwFrequencyMap = 1/freq (:364)
+      } else {
+        const long long key = ((long long)(int)uvw[k] * 1000003LL + (long long)(int)uvw[K + k]) * 1000003LL +
+                              (long long)(int)uvw[2 * K + k];
+        auto it = uvwmap.find(key);
+        wgt[k] = it != uvwmap.end() ? 1.0f / it->second : 1.0f;  // :458-470
+      }
+    }
+    const std::string sh_path = freq_dir + "shadeM" + std::to_string(p + 1) + dur + ".txt";
+    int64_t Ks = 0;
+    std::vector<int32_t> raw;
+    if (viss_text_read_ints(sh_path.c_str(), 4, nullptr, 0, &Ks) == VISS_OK) {
+      raw.resize((size_t)Ks * 4);
+      viss_text_read_ints(sh_path.c_str(), 4, raw.data(), Ks, &Ks);
+    }
+    if (Ks != K) std::printf("load wrong! uvw shape must be equal to shadeM shape\n");  // :402-406
+    std::vector<int32_t> M1(K, 0), M2(K, 0), M3(K, 0), M4(K, 0);
+    for (int64_t k = 0; k < K && k < Ks; ++k) {
+      const int32_t* r = &raw[4 * k];
+      M1[k] = std::min(r[0], r[1]) - 1; M2[k] = std::max(r[0], r[1]) - 1;
+      M3[k] = std::min(r[2], r[3]) - 1; M4[k] = std::max(r[2], r[3]) - 1;
+    }
+    std::vector<float> r1(K), r2(K);
+    for (int64_t k = 0; k < K; ++k) {
+      r1[k] = (float)M1[k] / (float)M2[k];
+      r2[k] = (float)M3[k] / (float)M4[k];
+    }
+    Dev<float> du, dv, dw, dwgt, dr1, dr2, dV, dF;
+    Dev<int32_t> dM1, dM2, dM3, dM4;
+    if (du.up(uvw.data(), K) || dv.up(uvw.data() + K, K) || dw.up(uvw.data() + 2 * K, K) || dwgt.up(wgt.data(), K) ||
+        dM1.up(M1.data(), K) || dM2.up(M2.data(), K) || dM3.up(M3.data(), K) || dM4.up(M4.data(), K) ||
+        dr1.up(r1.data(), K) || dr2.up(r2.data(), K) || dV.alloc(2 * K) || dF.alloc(2 * J)) {
+      std::fprintf(stderr, "device allocation failed\n");
+      return 1;
+    }
+    const double t1 = now();
+    const int var = variant == "plain" ? VISS_VARIANT_PLAIN : VISS_VARIANT_OPTIM;
+    CHECKV(viss_visscal((int)K, (int)J, RES, dFF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dM1.p, dM2.p, dM3.p,
+                        dM4.p, nullptr, nullptr, d, d, d, var, mask, precision, nullptr));
+    CHECKC(cudaDeviceSynchronize());
+    const double t2 = now();
+    CHECKV(viss_imagerecon((int)K, (int)J, RES, dF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dwgt.p, dr1.p,
+                           dr2.p, dr1.p, dr2.p, d, d, d, precision, nullptr));
+    CHECKC(cudaDeviceSynchronize());
+    const double t3 = now();
+    std::vector<float> F(2 * J);
+    CHECKC(cudaMemcpy(F.data(), dF.p, sizeof(float) * 2 * J, cudaMemcpyDeviceToHost));
+    std::string out;
+    if (tenM) {
+      const std::string suf = variant == "optim1" ? "_optim1" : variant == "optim2" ? "_optim2" : "";
+      out = outdir + "F" + std::to_string(p + 1) + "period10M" + suf + ".txt";
+      std::vector<float> re(J);
+      for (int64_t j = 0; j < J; ++j) re[j] = F[2 * j];
+      CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), J, J));
+    } else {
+      // expanded to the fine grid: F[NX[c]-1] (vissGen1M_shade_optim1.cu:680-684)
+      out = outdir + "F" + std::to_string(p + 1) + "_" + variant + ".txt";
+      std::vector<float> re(X);
+      for (int64_t c = 0; c < X; ++c) re[c] = F[2 * ((int64_t)NX[c] - 1)];
+      CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
+    }
+    const double t4 = now();
+    std::printf("Period %d Load UWV Cost Time is: %f s\n", p + 1, t1 - t0);
+    std::printf("Period %d Compute Viss Cost Time is: %f s\n", p + 1, t2 - t1);
+    std::printf("Period %d Image Reconstruction Cost Time is: %f s\n", p + 1, t3 - t2);
+    std::printf("Period %d Save Image Cost Time is: %f s (%s)\n", p + 1, t4 - t3, out.c_str());
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------ shade
+int shade(const Args& a, const std::string& which) {
+  const std::string root = a.get("root", ".");
+  int RES = which == "shade1M" ? 2094 : which == "shade10M" ? 20940 : 62820;
+  RES = (int)a.geti("res", RES);
+  const std::string dir = root + (which == "shade1M" ? "/frequency_1M/" : which == "shade10M" ? "/frequency_10M/"
+                                                                                               : "/frequency_30M/");
+  const std::string dur = which == "shade1M" ? "frequency1M" : which == "shade10M" ? "frequency10M" : "frequency30M";
+  // shade1M: periods 1..130 of uvw{p}; shade10M: updated_uvw{p}, p = 2..34 (its loop starts at
+  // tid+1, so period 1 is skipped, shade10M.cu:152); shade30M: one file uvw1 -> ./shade30Mperiod1.txt
+  const int first = (int)a.geti("first", which == "shade10M" ? 2 : 1);
+  const int last = (int)a.geti("last", which == "shade1M" ? 130 : which == "shade10M" ? 34 : 1);
+  for (int p = first; p <= last; ++p) {
+    const std::string in = dir + (which == "shade10M" ? "updated_uvw" : "uvw") + std::to_string(p) + dur + ".txt";
+    std::vector<float> uvw;
+    int64_t K = 0;
+    if (read_cols(in, which == "shade10M" ? 4 : 3, uvw, &K)) {
+      std::printf("address_uvw: %s (missing, skipped)\n", in.c_str());
+      continue;
+    }
+    Dev<float> du, dv, dw;
+    Dev<int32_t> dout;
+    Dev<char> ws;
+    const size_t wsb = viss_shade_windows_workspace(K);
+    if (du.up(uvw.data(), K) || dv.up(uvw.data() + K, K) || dw.up(uvw.data() + 2 * K, K) || dout.alloc(4 * K) ||
+        ws.alloc(wsb)) {
+      std::fprintf(stderr, "device allocation failed\n");
+      return 1;
+    }
+    double mean_r = 0;
+    CHECKV(viss_shade_windows(du.p, dv.p, dw.p, K, RES, a.getd("mean-r", 0.0), dout.p, &mean_r, ws.p, wsb, nullptr));
+    std::vector<int32_t> out(4 * K);
+    CHECKC(cudaMemcpy(out.data(), dout.p, sizeof(int32_t) * 4 * K, cudaMemcpyDeviceToHost));
+    const std::string op = which == "shade30M" ? root + "/shade30Mperiod1.txt"
+                                               : dir + "shadeM" + std::to_string(p) + dur + ".txt";
+    CHECKV(viss_text_write_ints(op.c_str(), 4, out.data(), K));
+    std::printf("period %d: %lld uvw, mean r %.6g, wrote %s\n", p, (long long)K, mean_r, op.c_str());
+  }
+  return 0;
+}
+
+// ------------------------------------------------------------------ MIncline
+int mincline(const Args& a) {
+  const std::string root = a.get("root", ".");
+  const int periods = (int)a.geti("periods", 34);
+  const int first = (int)a.geti("first", 1);
+  const double frequency = a.getd("frequency", 1e7);
+  const double stride = a.getd("stride", 0.01);
+  viss_orbit_cfg cfg{};
+  cfg.nsat = 8;
+  cfg.orbit_res = (int)(2.4 * 3600 * (int)(1.0 / stride));  // :185
+  cfg.orbit_res = (int)a.geti("orbit-res", cfg.orbit_res);
+  cfg.orbit_counts = (int)a.geti("orbit-counts", 140);
+  cfg.a_km = 2038.14; cfg.e = 0; cfg.incl_deg = 30; cfg.argp_deg = 0; cfg.raan_step_deg = 0.08;
+  static const float r1[8] = {0, 1e3, 4.45e3, 6e3, 9.1e3, 16.2e3, 35.3e3, 100e3};
+  static const float r2[8] = {0, 0.1e3, 0.445e3, 0.6e3, 0.91e3, 1.62e3, 3.53e3, 10e3};
+  cfg.r1_m = r1; cfg.r2_m = r2;
+  cfg.fp64 = 0;
+  const int lambda = (int)(3e8 / frequency);  // int lambda (:190)
+  const std::string dir = root + "/frequency_10M/";
+  mkdir_p(dir);
+  for (int index = first; index <= periods; ++index) {
+    cfg.index = index;
+    const int64_t S = viss_orbit_snapshots(&cfg);
+    const int P = 56;
+    const int64_t K = S * P;
+    Dev<float> pos, u, v, w, pu, pv, pw;
+    Dev<char> ws;
+    if (pos.alloc(S * 8 * 3) || u.alloc(K) || v.alloc(K) || w.alloc(K) || pu.alloc(K) || pv.alloc(K) || pw.alloc(K)) {
+      std::fprintf(stderr, "device allocation failed\n");
+      return 1;
+    }
+    CHECKV(viss_orbit_positions(&cfg, pos.p, nullptr, nullptr));
+    CHECKV(viss_baseline_uvw(pos.p, nullptr, S, 8, 1, (double)lambda, 1, u.p, v.p, w.p, nullptr, nullptr, nullptr));
+    // the reference concatenates the pairs' lists (pair-major) before its global sort
+    for (int q = 0; q < P; ++q) {
+      CHECKC(cudaMemcpy2D(pu.p + q * S, sizeof(float), u.p + q, sizeof(float) * P, sizeof(float), S,
+                          cudaMemcpyDeviceToDevice));
+      CHECKC(cudaMemcpy2D(pv.p + q * S, sizeof(float), v.p + q, sizeof(float) * P, sizeof(float), S,
+                          cudaMemcpyDeviceToDevice));
+      CHECKC(cudaMemcpy2D(pw.p + q * S, sizeof(float), w.p + q, sizeof(float) * P, sizeof(float), S,
+                          cudaMemcpyDeviceToDevice));
+    }
+    const size_t wsb = viss_dedup_uvw_workspace(K);
+    if (ws.alloc(wsb)) return 1;
+    int64_t cnt = 0;
+    CHECKV(viss_dedup_uvw(pu.p, pv.p, pw.p, K, &cnt, ws.p, wsb, nullptr));
+    std::vector<float> h(3 * cnt);
+    CHECKC(cudaMemcpy(h.data(), pu.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    CHECKC(cudaMemcpy(h.data() + cnt, pv.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    CHECKC(cudaMemcpy(h.data() + 2 * cnt, pw.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    const std::string out = dir + "uvw" + std::to_string(index) + "frequency10M.txt";
+    CHECKV(viss_text_write_floats(out.c_str(), 3, h.data(), cnt, cnt));
+    std::printf("period %d: %lld unique uvw of %lld -> %s\n", index, (long long)cnt, (long long)K, out.c_str());
+  }
+  return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  std::string prog = argv[0];
+  auto slash = prog.find_last_of('/');
+  if (slash != std::string::npos) prog = prog.substr(slash + 1);
+  int first = 1;
+  if (prog == "viss_dropin" && argc > 1) {
+    prog = argv[1];
+    first = 2;
+  }
+  const Args a = parse(argc, argv, first);
+  if (prog.rfind("vissGen10M", 0) == 0) {
+    Args b = a;
+    if (prog.find("optim1") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "optim1";
+    if (prog.find("optim2") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "optim2";
+    return vissgen(b, true);
+  }
+  if (prog.rfind("vissGen1M", 0) == 0) {
+    Args b = a;
+    if (prog.find("optim2") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "optim2";
+    return vissgen(b, false);
+  }
+  if (prog == "shade1M" || prog == "shade10M" || prog == "shade30M") return shade(a, prog);
+  if (prog.rfind("MIncline", 0) == 0) return mincline(a);
+  std::fprintf(stderr,
+               "usage: viss_dropin {vissGen10M_shade|vissGen10M_shade_optim1|vissGen10M_shade_optim2|"
+               "vissGen1M_shade_optim1|vissGen1M_shade_optim2|shade1M|shade10M|shade30M|"
+               "MIncline_generate_uvw_float} [--root DIR] [--flag value ...]\n");
+  return 2;
+}

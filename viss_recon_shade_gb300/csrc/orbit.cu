@@ -32,8 +32,9 @@ struct OrbitDev {
 
 // uvwPosition (:113-151) index arithmetic for snapshot g: the global sample
 // `circle` of the satellite's array, or zero-fill (kind 1), or the reference's
-// read of one element past the satellite's array (kind 2: the next satellite's
-// first sample; zero for the last satellite).
+// read of one element past the satellite's array (kind 2): that is the next
+// satellite's slot, not yet computed when uvwPosition runs for this satellite
+// (:224-308), so it reads zero as well.
 __device__ __forceinline__ int window_index(const OrbitDev& o, int64_t g, int64_t* circle) {
   const int64_t k = g / o.span + 1;
   const int64_t offset = (k - 1) * o.interval;
@@ -113,18 +114,15 @@ __global__ void orbit_positions_kernel(const OrbitDev o, float* pos, double* pos
   const int sat = (int)(t % o.nsat);
   int64_t circle;
   const int kind = window_index(o, g, &circle);
-  int src_sat = sat;
-  int64_t src = circle;
-  bool zero = kind == 1 || (kind == 2 && sat + 1 >= o.nsat);
-  if (kind == 2 && !zero) { src_sat = sat + 1; src = 0; }
+  const bool zero = kind != 0;
   if (o.fp64) {
     double p[3] = {0.0, 0.0, 0.0};
-    if (!zero) position_f64(o, src_sat, src, p);
+    if (!zero) position_f64(o, sat, circle, p);
     pos[3 * t] = (float)p[0]; pos[3 * t + 1] = (float)p[1]; pos[3 * t + 2] = (float)p[2];
     if (pos64) { pos64[3 * t] = p[0]; pos64[3 * t + 1] = p[1]; pos64[3 * t + 2] = p[2]; }
   } else {
     float p[3] = {0.f, 0.f, 0.f};
-    if (!zero) position_f32(o, src_sat, src, p);
+    if (!zero) position_f32(o, sat, circle, p);
     pos[3 * t] = p[0]; pos[3 * t + 1] = p[1]; pos[3 * t + 2] = p[2];
     if (pos64) { pos64[3 * t] = p[0]; pos64[3 * t + 1] = p[1]; pos64[3 * t + 2] = p[2]; }
   }

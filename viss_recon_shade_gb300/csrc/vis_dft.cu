@@ -42,20 +42,32 @@ __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const flo
   ai = fmaf(c, sn, ai);
 }
 
+// Exact decision near the limb (rare): kept out of line so its double-precision
+// registers do not weigh on the hot loops.
+__device__ __noinline__ bool geo_exact_at(const VisParams& p, int j, int gidx) {
+  return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
+}
+
 // fast geometric test against one satellite: s_hat . p_hat + cos(alpha) < 0,
 // re-decided exactly near the limb.
 __device__ __forceinline__ bool geo_test(const float4& g, const float4& d, int gidx, const VisParams& p) {
   const float e = fmaf(g.x, d.x, fmaf(g.y, d.y, fmaf(g.z, d.z, d.w)));
   if (fabsf(e) >= GEO_EPS) return e < 0.f;
-  const int j = __float_as_int(g.w);
-  return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
+  return geo_exact_at(p, __float_as_int(g.w), gidx);
 }
+
+__device__ __noinline__ bool ref_hit_general(int4 wv, int64_t j, int res);
 
 // REF window membership of fine pixel (q, r) / index j for window {lo_a, lo_b, M1, M2}.
 __device__ __forceinline__ bool ref_hit(const int4& wv, int q, int r, int64_t j, int res) {
   if (wv.x > wv.y) return false;
   if (wv.z + 1 >= 0 && wv.w <= res) return q >= wv.x && q <= wv.y && r > wv.z && r < wv.w;
-  // general: exists lo in [lo_a, lo_b] with lo*res + M1 + 1 <= j < lo*res + M2
+  return ref_hit_general(wv, j, res);
+}
+
+// windows whose column range is not inside one row
+__device__ __noinline__ bool ref_hit_general(int4 wv, int64_t j, int res) {
+  // exists lo in [lo_a, lo_b] with lo*res + M1 + 1 <= j < lo*res + M2
   const int64_t hi_num = j - wv.z - 1, lo_num = j - wv.w + 1;
   int64_t lo_max = hi_num >= 0 ? hi_num / res : -((-hi_num + res - 1) / res);     // floor
   int64_t lo_min = lo_num >= 0 ? (lo_num + res - 1) / res : -((-lo_num) / res);   // ceil
@@ -73,6 +85,7 @@ struct VisSmem {
   float4 lo[COMP ? VIS_P : 1];
   float4 geo[GEO ? VIS_P : 1];
   int2 qr[REF ? VIS_P : 1];
+  int4 win[REF ? VIS_ROWS : 1];   // the block's REF windows, read in masked tiles only
   int wcnt[VIS_THREADS / 32][2];
 };
 
@@ -91,27 +104,34 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   const int64_t row0 = (int64_t)blockIdx.x * VIS_ROWS;
   const int split = blockIdx.y;
 
-  int U[VIS_TK], V[VIS_TK], W[VIS_TK], GM[VIS_TK];
-  int FU[VIS_TK], FV[VIS_TK], FW[VIS_TK], GN[VIS_TK];
+  // Registers per visibility: fixed-point U,V,W [+ fractional F] [+ float U for
+  // the compensation] and the two accumulators.  Satellite indices (geometric)
+  // and windows (REF) are fetched only on the masked paths.
+  int U[VIS_TK], V[VIS_TK], W[VIS_TK];
+  int FU[VIS_TK], FV[VIS_TK], FW[VIS_TK];
   float UF[VIS_TK], VF[VIS_TK], WF[VIS_TK];
-  int4 WIN[REF ? VIS_TK : 1];
   float ar[VIS_TK], ai[VIS_TK];
+  bool any_win = false;
 #pragma unroll
   for (int i = 0; i < VIS_TK; ++i) {
     const int64_t k = row0 + tid + i * VIS_THREADS;  // rows are padded to a whole block
     const int4 r0 = p.rows0[k];
-    U[i] = r0.x; V[i] = r0.y; W[i] = r0.z; GM[i] = r0.w;
-    FU[i] = FV[i] = FW[i] = 0; GN[i] = 0;
-    if (FRAC || GEO) {
+    U[i] = r0.x; V[i] = r0.y; W[i] = r0.z;
+    FU[i] = FV[i] = FW[i] = 0;
+    if (FRAC) {
       const int4 r1 = p.rows1[k];
-      FU[i] = r1.x; FV[i] = r1.y; FW[i] = r1.z; GN[i] = r1.w;
+      FU[i] = r1.x; FV[i] = r1.y; FW[i] = r1.z;
     }
     UF[i] = VF[i] = WF[i] = 0.f;
     if (COMP) {
       const float4 f = p.rowsf[k];
       UF[i] = f.x; VF[i] = f.y; WF[i] = f.z;
     }
-    if (REF) WIN[i] = p.win[k];
+    if (REF) {
+      const int4 wv = p.win[k];
+      sm.win[tid + i * VIS_THREADS] = wv;
+      any_win |= wv.x <= wv.y && wv.z + 1 < wv.w;
+    }
     ar[i] = 0.f; ai[i] = 0.f;
   }
   float4 cone0 = make_float4(0.f, 0.f, 0.f, 2.f), cone1 = make_float4(-2.f, 0.f, 0.f, 0.f);
@@ -131,37 +151,27 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
     int nfast = np, nmix = 0;
     bool masked_tile = false;
     if (GEO) {
+      // pass 1: classify against the block's bounding cone (only the class is
+      // kept across the barrier); pass 2: re-read the records (L2) and place them.
       constexpr int Q = VIS_P / VIS_THREADS;
-      bool isF[Q], isM[Q];
-      int4 a[Q], b[Q];
-      float4 lo[Q], g[Q];
+      unsigned cls = 0;  // 2 bits per slot: 1 fast, 2 mixed
 #pragma unroll
       for (int qq = 0; qq < Q; ++qq) {
         const int i = tid + qq * VIS_THREADS;
-        isF[qq] = isM[qq] = false;
         if (i < np) {
-          const int64_t j = tile + i;
-          a[qq] = p.pix0[j];
-          if (FRAC) b[qq] = p.pix1[j];
-          if (COMP) lo[qq] = p.plo[j];
-          g[qq] = p.pgeo[j];
-          const float d = fmaf(g[qq].x, cone0.x, fmaf(g[qq].y, cone0.y, g[qq].z * cone0.z));
-          if (d > cone0.w) {  // occluded for every row of the block
-            a[qq].w = __float_as_int(occ_val);
-            isF[qq] = occ_val != 0.f;
-          } else if (d < cone1.x) {  // visible for every row
-            isF[qq] = true;
-          } else {
-            isM[qq] = true;
-          }
+          const float4 g = p.pgeo[tile + i];
+          const float d = fmaf(g.x, cone0.x, fmaf(g.y, cone0.y, g.z * cone0.z));
+          if (d > cone0.w) cls |= (occ_val != 0.f ? 1u : 0u) << (2 * qq);  // occluded for every row
+          else if (d < cone1.x) cls |= 1u << (2 * qq);                      // visible for every row
+          else cls |= 2u << (2 * qq);
         }
       }
       unsigned bF[Q], bM[Q];
       int cf = 0, cm = 0;
 #pragma unroll
       for (int qq = 0; qq < Q; ++qq) {
-        bF[qq] = __ballot_sync(0xffffffffu, isF[qq]);
-        bM[qq] = __ballot_sync(0xffffffffu, isM[qq]);
+        bF[qq] = __ballot_sync(0xffffffffu, ((cls >> (2 * qq)) & 3u) == 1u);
+        bM[qq] = __ballot_sync(0xffffffffu, ((cls >> (2 * qq)) & 3u) == 2u);
         cf += __popc(bF[qq]);
         cm += __popc(bM[qq]);
       }
@@ -177,18 +187,18 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
       const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
       for (int qq = 0; qq < Q; ++qq) {
-        if (isF[qq]) {
-          const int pos = offF + __popc(bF[qq] & lt);
-          s_p0[pos] = a[qq];
-          if (FRAC) s_p1[pos] = b[qq];
-          if (COMP) s_lo[pos] = lo[qq];
-        }
-        if (isM[qq]) {
-          const int pos = VIS_P - 1 - (offM + __popc(bM[qq] & lt));
-          s_p0[pos] = a[qq];
-          if (FRAC) s_p1[pos] = b[qq];
-          if (COMP) s_lo[pos] = lo[qq];
-          s_geo[pos] = g[qq];
+        const unsigned c = (cls >> (2 * qq)) & 3u;
+        if (c) {
+          const int64_t j = tile + tid + qq * VIS_THREADS;
+          int4 a = p.pix0[j];
+          const float4 g = p.pgeo[j];
+          const float d = fmaf(g.x, cone0.x, fmaf(g.y, cone0.y, g.z * cone0.z));
+          if (c == 1u && d > cone0.w) a.w = __float_as_int(occ_val);
+          const int pos = c == 1u ? offF + __popc(bF[qq] & lt) : VIS_P - 1 - (offM + __popc(bM[qq] & lt));
+          s_p0[pos] = a;
+          if (FRAC) s_p1[pos] = p.pix1[j];
+          if (COMP) s_lo[pos] = p.plo[j];
+          if (c == 2u) s_geo[pos] = g;
         }
         offF += __popc(bF[qq]);
         offM += __popc(bM[qq]);
@@ -205,11 +215,11 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         if (REF) s_qr[i] = p.pqr[j];
       }
       bool hit = false;
-      if (REF) {
+      if (REF && any_win) {
         // bounding fine-index range of each window against [tile, tile + np)
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const int4 wv = WIN[i];
+          const int4 wv = sm.win[tid + i * VIS_THREADS];
           if (wv.x <= wv.y && wv.z + 1 < wv.w) {
             const int64_t lo_idx = (int64_t)wv.x * p.res + wv.z + 1;
             const int64_t hi_idx = (int64_t)wv.y * p.res + wv.w - 1;
@@ -245,13 +255,20 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         const float c0 = __int_as_float(a.w);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const float c = ref_hit(WIN[i], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
+          const float c = ref_hit(sm.win[tid + i * VIS_THREADS], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
           vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
                                ar[i], ai[i]);
         }
       }
     }
-    if (GEO) {
+    if (GEO && nmix > 0) {
+      int gm[VIS_TK], gn[VIS_TK];
+#pragma unroll
+      for (int i = 0; i < VIS_TK; ++i) {
+        const int64_t k = row0 + tid + i * VIS_THREADS;
+        gm[i] = __ldg(&p.rows0[k].w);
+        gn[i] = __ldg(&p.rows1[k].w);
+      }
       for (int mi = 0; mi < nmix; ++mi) {
         const int pi = VIS_P - 1 - mi;
         const int4 a = s_p0[pi];
@@ -263,9 +280,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         const float c0 = __int_as_float(a.w);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const float4 dm = __ldg(p.satdir + GM[i]);
-          const float4 dn = __ldg(p.satdir + GN[i]);
-          const bool occ = geo_test(g, dm, GM[i], p) || geo_test(g, dn, GN[i], p);
+          const float4 dm = __ldg(p.satdir + gm[i]);
+          const float4 dn = __ldg(p.satdir + gn[i]);
+          const bool occ = geo_test(g, dm, gm[i], p) || geo_test(g, dn, gn[i], p);
           const float c = occ ? occ_val : c0;
           if (c != 0.f)
             vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
@@ -290,7 +307,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 // fractional term; the row prep sets flags[0] when any uvw is fractional and
 // the kernel picks its loop from that flag (uniform branch, no host sync).
 template <int MASK, bool COMP>
-__global__ void __launch_bounds__(VIS_THREADS, 3) vis_fast_kernel(const VisParams p) {
+__global__ void __launch_bounds__(VIS_THREADS, 2) vis_fast_kernel(const VisParams p) {
   __shared__ VisSmem<MASK, COMP> sm;
   if (__ldg(p.flags) != 0) vis_body<MASK, true, COMP>(p, sm);
   else vis_body<MASK, false, COMP>(p, sm);
