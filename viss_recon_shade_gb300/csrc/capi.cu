@@ -52,6 +52,7 @@ struct VisPlan {
   void layout(void* ws) {
     Carver c(ws);
     flags = c.take<int>(64);
+    if (plain && geo) satdir = c.take<float4>(nsd);
     if (!plain) {
       pix0 = c.take<int4>(Jpad);
       pix1 = c.take<int4>(Jpad);
@@ -104,6 +105,9 @@ struct RecPlan {
   float2 *y = nullptr, *partial = nullptr;
   float* ratios = nullptr;
   int* flags = nullptr;
+  int32_t* perm = nullptr;
+  char* order_scratch = nullptr;
+  size_t order_bytes = 0;
   size_t bytes = 0;
 
   void layout(void* ws) {
@@ -111,7 +115,13 @@ struct RecPlan {
     flags = c.take<int>(64);
     if (plain) {
       if (ref) ratios = c.take<float>(2 * (size_t)Kpad);
+      if (geo) satdir = c.take<float4>(nsd);
     } else {
+      if (geo) {
+        perm = c.take<int32_t>(J > 0 ? J : 1);
+        order_bytes = pixel_order_scratch(J);
+        order_scratch = c.take<char>(order_bytes);
+      }
       pix0 = c.take<int4>(Jpad);
       pix1 = c.take<int4>(Jpad);
       if (comp) plo = c.take<float4>(Jpad);
@@ -214,8 +224,11 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
     VISS_CUDA(cudaMemsetAsync(V, 0, sizeof(float2) * (size_t)vis.K, st));
     return VISS_OK;
   }
-  if (p.plain) return launch_vis_plain(cfg, sky, vis, geo, dlmn, reinterpret_cast<float2*>(V), st);
   p.layout(ws);
+  if (p.plain) {
+    if (p.geo && (rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
+    return launch_vis_plain(cfg, sky, vis, geo, p.satdir, dlmn, reinterpret_cast<float2*>(V), st);
+  }
   VISS_CUDA(cudaMemsetAsync(p.flags, 0, 64 * sizeof(int), st));
   PixPrepArgs pa{};
   pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = sky.bright;
@@ -278,9 +291,14 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
       }
       ratios = p.ratios;
     }
-    return launch_recon_plain(cfg, sky, vis, geo, V, ratios, dlmn, reinterpret_cast<float2*>(F), st);
+    if (p.geo && (rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
+    return launch_recon_plain(cfg, sky, vis, geo, V, ratios, p.satdir, dlmn, reinterpret_cast<float2*>(F), st);
+  }
+  if (p.geo) {
+    if ((rc = pixel_order(sky.l, sky.m, sky.n, sky.J, p.order_scratch, p.order_bytes, p.perm, st))) return rc;
   }
   PixPrepArgs pa{};
+  pa.perm = p.perm;
   pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = nullptr;
   pa.J = sky.J; pa.Jpad = p.Jpad;
   pa.sl = scale[0]; pa.sm = scale[1]; pa.sn = scale[2]; pa.n_offset = cfg.n_offset;
@@ -310,13 +328,14 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   rp.satdir = p.satdir; rp.scones = p.scones;
   rp.l = sky.l; rp.m = sky.m; rp.n = sky.n; rp.sat_pos = geo ? geo->sat_pos : nullptr;
   rp.flags = p.flags;
+  rp.perm = p.perm;
   rp.out = p.nsplit > 1 ? p.partial : reinterpret_cast<float2*>(F);
   rp.K = vis.K; rp.J = sky.J; rp.kchunk = p.kchunk; rp.nsplit = p.nsplit;
   rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
   rp.norm = (float)cfg.norm; rp.recon_mask = cfg.recon_mask;
   if ((rc = launch_recon_fast(rp, p.npb, p.comp, st))) return rc;
   if (p.nsplit > 1)
-    return launch_recon_reduce(p.partial, p.nsplit, sky.J, (float)cfg.norm, reinterpret_cast<float2*>(F), st);
+    return launch_recon_reduce(p.partial, p.nsplit, sky.J, (float)cfg.norm, p.perm, reinterpret_cast<float2*>(F), st);
   return VISS_OK;
 }
 

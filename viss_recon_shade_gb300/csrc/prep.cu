@@ -10,17 +10,20 @@ namespace viss {
 // ------------------------------------------------------------- pixels
 // Pixel j: phase coordinates x = s*l, y = s*m, z = s*(n + n_offset) in turns per
 // wavelength, evaluated in double from the float inputs.
+// Records are written at position `pos`; with a permutation the pixel at pos
+// is perm[pos] (records keep the original index in rec1.w / geo.w).
 __global__ void prep_pixels_kernel(PixPrepArgs a) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= a.Jpad) return;
-  if (j >= a.J) {
-    a.rec0[j] = make_int4(0, 0, 0, 0);
-    if (a.rec1) a.rec1[j] = make_int4(0, 0, 0, (int)j);
-    if (a.lo) a.lo[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a.geo) a.geo[j] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)j));
-    if (a.qr) a.qr[j] = make_int2(-1, -1);
+  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= a.Jpad) return;
+  if (pos >= a.J) {
+    a.rec0[pos] = make_int4(0, 0, 0, 0);
+    if (a.rec1) a.rec1[pos] = make_int4(0, 0, 0, (int)pos);
+    if (a.lo) a.lo[pos] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.geo) a.geo[pos] = make_float4(0.f, 0.f, 0.f, __int_as_float((int)pos));
+    if (a.qr) a.qr[pos] = make_int2(-1, -1);
     return;
   }
+  const int64_t j = a.perm ? (int64_t)a.perm[pos] : pos;
   const double x = a.sl * (double)a.l[j];
   const double y = a.sm * (double)a.m[j];
   const double z = a.sn * ((double)a.n[j] + a.n_offset);
@@ -30,27 +33,67 @@ __global__ void prep_pixels_kernel(PixPrepArgs a) {
     if (a.trunc) b = (float)(int)b;  // int addFF = FF[..] (vissGen10M_shade.cu:128)
   }
   const uint32_t A = fix32(x), B = fix32(y), C = fix32(z);
-  a.rec0[j] = make_int4((int)A, (int)B, (int)C, __float_as_int(b));
+  a.rec0[pos] = make_int4((int)A, (int)B, (int)C, __float_as_int(b));
   if (a.rec1) {
-    a.rec1[j] = make_int4((int)llrint(x * 1073741824.0), (int)llrint(y * 1073741824.0),
+    a.rec1[pos] = make_int4((int)llrint(x * 1073741824.0), (int)llrint(y * 1073741824.0),
                           (int)llrint(z * 1073741824.0), (int)j);
   }
   if (a.lo) {
     const double sc = 4294967296.0;
     const double xa = x * sc, ya = y * sc, za = z * sc;
-    a.lo[j] = make_float4((float)((xa - rint(xa)) / sc), (float)((ya - rint(ya)) / sc),
+    a.lo[pos] = make_float4((float)((xa - rint(xa)) / sc), (float)((ya - rint(ya)) / sc),
                           (float)((za - rint(za)) / sc), 0.f);
   }
   if (a.geo) {
     const double gx = a.l[j], gy = a.m[j], gz = a.n[j];
     const double nn = sqrt(gx * gx + gy * gy + gz * gz);
     const double inv = nn > 0 ? 1.0 / nn : 0.0;
-    a.geo[j] = make_float4((float)(gx * inv), (float)(gy * inv), (float)(gz * inv), __int_as_float((int)j));
+    a.geo[pos] = make_float4((float)(gx * inv), (float)(gy * inv), (float)(gz * inv), __int_as_float((int)j));
   }
   if (a.qr) {
     const int res = a.res > 0 ? a.res : 1;
-    a.qr[j] = make_int2((int)(j / res), (int)(j % res));
+    a.qr[pos] = make_int2((int)(j / res), (int)(j % res));
   }
+}
+
+// ------------------------------------------------------------- pixel order
+// Spatial order of the sky for the geometric mask: the direction is projected
+// on the face of the cube it points to and the face coordinates (10 bits each)
+// are interleaved (Morton), so consecutive positions are neighbouring pixels
+// and a warp's pixels see the Moon's limb together.
+__device__ __forceinline__ uint32_t spread10(uint32_t x) {
+  x &= 0x3ff;
+  x = (x | (x << 16)) & 0x030000ff;
+  x = (x | (x << 8)) & 0x0300f00f;
+  x = (x | (x << 4)) & 0x030c30c3;
+  x = (x | (x << 2)) & 0x09249249;
+  return x;
+}
+
+__global__ void pixel_keys_kernel(const float* l, const float* m, const float* n, int64_t J, uint32_t* keys,
+                                  int32_t* idx) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= J) return;
+  const float x = l[j], y = m[j], z = n[j];
+  const float ax = fabsf(x), ay = fabsf(y), az = fabsf(z);
+  uint32_t face;
+  float a, b, d;
+  if (ax >= ay && ax >= az) { face = x >= 0 ? 0 : 1; a = y; b = z; d = ax; }
+  else if (ay >= az) { face = y >= 0 ? 2 : 3; a = x; b = z; d = ay; }
+  else { face = z >= 0 ? 4 : 5; a = x; b = y; d = az; }
+  const float inv = d > 0.f ? 1.0f / d : 0.f;
+  const uint32_t ia = (uint32_t)fminf(1023.f, fmaxf(0.f, (a * inv + 1.0f) * 511.5f));
+  const uint32_t ib = (uint32_t)fminf(1023.f, fmaxf(0.f, (b * inv + 1.0f) * 511.5f));
+  keys[j] = (face << 20) | (spread10(ia) << 1) | spread10(ib);
+  idx[j] = (int32_t)j;
+}
+
+int launch_pixel_keys(const float* l, const float* m, const float* n, int64_t J, uint32_t* keys, int32_t* idx,
+                      cudaStream_t st) {
+  if (J <= 0) return VISS_OK;
+  pixel_keys_kernel<<<(unsigned)((J + 255) / 256), 256, 0, st>>>(l, m, n, J, keys, idx);
+  VISS_LAUNCH_CHECK("pixel_keys_kernel");
+  return VISS_OK;
 }
 
 int launch_prep_pixels(const PixPrepArgs& a, cudaStream_t st) {

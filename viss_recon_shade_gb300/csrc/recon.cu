@@ -20,6 +20,11 @@
 
 namespace viss {
 
+// Exact decision near the limb (rare), out of line.
+__device__ __noinline__ bool geo_exact_pix(const ReconParams& p, int j, int gidx) {
+  return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
+}
+
 template <bool FRAC, bool COMP>
 __device__ __forceinline__ void rec_term(const int4& r0, const int4& r1, const float4& rf, float2 y, int A, int B,
                                          int C, int Ap, int Bp, int Cp, float lx, float ly, float lz, float& fr,
@@ -44,6 +49,8 @@ __device__ __forceinline__ void rec_term(const int4& r0, const int4& r1, const f
 }
 
 constexpr int RM_NONE = 0, RM_REF = 1, RM_GEO = 2;
+constexpr int REC_SAT_CACHE = 1024;  // satellite directions cached per tile (float4)
+constexpr int REC_CONE_CACHE = 128;  // snapshot cones cached per tile
 
 template <int RM, bool COMP>
 struct RecSmem {
@@ -54,42 +61,66 @@ struct RecSmem {
   int4 win[RM == RM_REF ? REC_Q : 1];
   int snap[RM == RM_GEO ? REC_Q : 1];
   int runend[RM == RM_GEO ? REC_Q : 1];
+  float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
+  float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
+  int srange[2];
 };
+
+// s += x with the rounding error of the sum carried in c (Kahan).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
 
 template <int RM, bool FRAC, bool COMP>
 __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm) {
   const int tid = threadIdx.x;
-  const int64_t j0 = (int64_t)blockIdx.x * REC_PIX;
+  // a warp owns 32 * REC_TJ consecutive positions: with the spatial order of
+  // the geometric passes that is one compact patch of sky
+  const int64_t j0 = (int64_t)blockIdx.x * REC_PIX + (int64_t)tid * REC_TJ;
   int A[REC_TJ], B[REC_TJ], C[REC_TJ], Ap[REC_TJ], Bp[REC_TJ], Cp[REC_TJ];
   float LX[REC_TJ], LY[REC_TJ], LZ[REC_TJ];
   float GX[REC_TJ], GY[REC_TJ], GZ[REC_TJ];
   int TP[REC_TJ], PP[REC_TJ], JJ[REC_TJ];
-  float fr[REC_TJ], fi[REC_TJ];
+  float fr[REC_TJ], fi[REC_TJ];    // running totals (Kahan)
+  float cr[REC_TJ], ci[REC_TJ];    // their compensation
 #pragma unroll
   for (int i = 0; i < REC_TJ; ++i) {
-    const int64_t j = j0 + tid + i * REC_THREADS;  // pixels padded to a whole block
-    JJ[i] = (int)j;
-    const int4 a = p.pix0[j];
+    const int64_t pos = j0 + i;  // pixels padded to a whole block
+    const int4 a = p.pix0[pos];
     A[i] = a.x; B[i] = a.y; C[i] = a.z;
     Ap[i] = Bp[i] = Cp[i] = 0;
-    if (FRAC) { const int4 b = p.pix1[j]; Ap[i] = b.x; Bp[i] = b.y; Cp[i] = b.z; }
+    JJ[i] = (int)pos;
+    if (FRAC || RM == RM_GEO) {
+      const int4 b = p.pix1[pos];
+      Ap[i] = b.x; Bp[i] = b.y; Cp[i] = b.z;
+      JJ[i] = b.w;  // original pixel index
+    }
     LX[i] = LY[i] = LZ[i] = 0.f;
-    if (COMP) { const float4 lo = p.plo[j]; LX[i] = lo.x; LY[i] = lo.y; LZ[i] = lo.z; }
+    if (COMP) { const float4 lo = p.plo[pos]; LX[i] = lo.x; LY[i] = lo.y; LZ[i] = lo.z; }
     GX[i] = GY[i] = GZ[i] = 0.f;
-    if (RM == RM_GEO) { const float4 g = p.pgeo[j]; GX[i] = g.x; GY[i] = g.y; GZ[i] = g.z; }
+    if (RM == RM_GEO) { const float4 g = p.pgeo[pos]; GX[i] = g.x; GY[i] = g.y; GZ[i] = g.z; }
     TP[i] = PP[i] = -1;
-    if (RM == RM_REF) { const int2 qr = p.pqr[j]; PP[i] = qr.x; TP[i] = qr.y; }
-    fr[i] = 0.f; fi[i] = 0.f;
+    if (RM == RM_REF) { const int2 qr = p.pqr[pos]; PP[i] = qr.x; TP[i] = qr.y; }
+    fr[i] = fi[i] = cr[i] = ci[i] = 0.f;
   }
+  bool valid[REC_TJ];
+#pragma unroll
+  for (int i = 0; i < REC_TJ; ++i) valid[i] = j0 + i < p.J;
   const int64_t kb = (int64_t)blockIdx.y * p.kchunk;
   int64_t ke = kb + p.kchunk;
   if (ke > p.K) ke = p.K;
-  int64_t jlast = j0 + REC_PIX - 1;
+  const int64_t jfirst = (int64_t)blockIdx.x * REC_PIX;
+  int64_t jlast = jfirst + REC_PIX - 1;
   if (jlast > p.J - 1) jlast = p.J - 1;
 
   for (int64_t tile = kb; tile < ke; tile += REC_Q) {
     const int nq = (int)((ke - tile) < REC_Q ? (ke - tile) : REC_Q);
     __syncthreads();
+    if (RM == RM_GEO && tid == 0) { sm.srange[0] = 0x7fffffff; sm.srange[1] = -1; }
+    if (RM == RM_GEO) __syncthreads();
     bool hit = false;
     for (int r = tid; r < nq; r += REC_THREADS) {
       const int64_t k = tile + r;
@@ -103,34 +134,48 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         sm.win[r] = wv;
         if (wv.x >= 1 && wv.y >= 1) {
           const int64_t lo_idx = (int64_t)p.res + 1, hi_idx = (int64_t)wv.y * p.res + wv.x;
-          if (lo_idx <= jlast && hi_idx >= j0) hit = true;
+          if (lo_idx <= jlast && hi_idx >= jfirst) hit = true;
         }
       }
-      if (RM == RM_GEO) sm.snap[r] = r0.w / p.nsat;
+      if (RM == RM_GEO) {
+        const int sn = r0.w / p.nsat;
+        sm.snap[r] = sn;
+        atomicMin(&sm.srange[0], sn);
+        atomicMax(&sm.srange[1], sn);
+      }
     }
     const bool masked_tile = __syncthreads_or(hit) != 0;
+    float tr[REC_TJ], ti[REC_TJ];  // this tile's sums
+#pragma unroll
+    for (int i = 0; i < REC_TJ; ++i) tr[i] = ti[i] = 0.f;
     if (RM == RM_GEO) {
+      const int s_lo = sm.srange[0], s_hi = sm.srange[1];
+      const int nsn = s_hi - s_lo + 1;
+      const bool cached = nsn <= REC_CONE_CACHE && nsn * p.nsat <= REC_SAT_CACHE;
+      if (cached) {
+        for (int t = tid; t < nsn * p.nsat; t += REC_THREADS) sm.sat[t] = p.satdir[(int64_t)s_lo * p.nsat + t];
+        for (int t = tid; t < 2 * nsn; t += REC_THREADS) sm.cone[t] = p.scones[2 * (int64_t)s_lo + t];
+      }
       for (int r = tid; r < nq; r += REC_THREADS) {
-        const int s = sm.snap[r];
-        if (r == 0 || sm.snap[r - 1] != s) {
+        const int sn = sm.snap[r];
+        if (r == 0 || sm.snap[r - 1] != sn) {
           int e = r + 1;
-          while (e < nq && sm.snap[e] == s) ++e;
+          while (e < nq && sm.snap[e] == sn) ++e;
           sm.runend[r] = e;
         }
       }
       __syncthreads();
       for (int r = 0; r < nq;) {
         const int re = sm.runend[r];
-        const int s = sm.snap[r];
-        const float4 c0 = __ldg(p.scones + 2 * (int64_t)s);
-        const float c1 = __ldg(p.scones + 2 * (int64_t)s + 1).x;
+        const int sn = sm.snap[r];
+        const float4 c0 = cached ? sm.cone[2 * (sn - s_lo)] : __ldg(p.scones + 2 * (int64_t)sn);
+        const float c1 = cached ? sm.cone[2 * (sn - s_lo) + 1].x : __ldg(p.scones + 2 * (int64_t)sn + 1).x;
         bool all_vis = true, all_occ = true;
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i) {
           const float d = fmaf(GX[i], c0.x, fmaf(GY[i], c0.y, GZ[i] * c0.z));
-          const bool valid = JJ[i] < p.J;
-          all_vis &= (!valid) || d < c1;
-          all_occ &= (!valid) || d > c0.w;
+          all_vis &= (!valid[i]) || d < c1;
+          all_occ &= (!valid[i]) || d > c0.w;
         }
         const bool wocc = __all_sync(0xffffffffu, all_occ);
         const bool wvis = __all_sync(0xffffffffu, all_vis);
@@ -147,24 +192,21 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i)
               rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
-                                   fr[i], fi[i]);
+                                   tr[i], ti[i]);
           }
         } else {
-          // per-pixel satellite occlusion bits for snapshot s
+          // per-pixel satellite occlusion bits for snapshot sn
           uint32_t bits[REC_TJ];
-          const int g0 = s * p.nsat;
+          const int g0 = sn * p.nsat;
 #pragma unroll
           for (int i = 0; i < REC_TJ; ++i) bits[i] = 0u;
           for (int sat = 0; sat < p.nsat; ++sat) {
-            const float4 d = __ldg(p.satdir + g0 + sat);
+            const float4 d = cached ? sm.sat[(sn - s_lo) * p.nsat + sat] : __ldg(p.satdir + g0 + sat);
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i) {
               const float e = fmaf(GX[i], d.x, fmaf(GY[i], d.y, fmaf(GZ[i], d.z, d.w)));
               bool occ = e < 0.f;
-              if (fabsf(e) < GEO_EPS && JJ[i] < p.J) {
-                const int j = JJ[i];
-                occ = geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)(g0 + sat), p.R);
-              }
+              if (fabsf(e) < GEO_EPS && valid[i]) occ = geo_exact_pix(p, JJ[i], g0 + sat);
               bits[i] |= (occ ? 1u : 0u) << sat;
             }
           }
@@ -179,7 +221,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
             for (int i = 0; i < REC_TJ; ++i) {
               const float2 yy = (bits[i] & pm) ? make_float2(0.f, 0.f) : y;
               rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
-                                   fr[i], fi[i]);
+                                   tr[i], ti[i]);
             }
           }
         }
@@ -198,8 +240,8 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         for (int i = 0; i < REC_TJ; ++i) {
           const bool skip = TP[i] >= 1 && TP[i] <= wv.x && PP[i] >= 1 && PP[i] <= wv.y;
           const float2 yy = skip ? make_float2(0.f, 0.f) : y;
-          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], fr[i],
-                               fi[i]);
+          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], tr[i],
+                               ti[i]);
         }
       }
     } else {
@@ -213,18 +255,27 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         const float2 y = sm.y[rr];
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i)
-          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], fr[i],
-                               fi[i]);
+          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], tr[i],
+                               ti[i]);
       }
+    }
+#pragma unroll
+    for (int i = 0; i < REC_TJ; ++i) {
+      kahan_add(fr[i], cr[i], tr[i]);
+      kahan_add(fi[i], ci[i], ti[i]);
     }
   }
   // F = norm * (-fr - i fi)  (the angle carried an extra half turn)
 #pragma unroll
   for (int i = 0; i < REC_TJ; ++i) {
-    const int64_t j = j0 + tid + i * REC_THREADS;
-    if (j < p.J) {
-      if (p.nsplit == 1) p.out[j] = make_float2(-fr[i] * p.norm, -fi[i] * p.norm);
-      else p.out[(int64_t)blockIdx.y * p.J + j] = make_float2(fr[i], fi[i]);
+    const int64_t pos = j0 + i;
+    if (pos < p.J) {
+      if (p.nsplit == 1) {
+        const int64_t j = p.perm ? (int64_t)p.perm[pos] : pos;
+        p.out[j] = make_float2(-fr[i] * p.norm, -fi[i] * p.norm);
+      } else {
+        p.out[(int64_t)blockIdx.y * p.J + pos] = make_float2(fr[i], fi[i]);
+      }
     }
   }
 }
@@ -255,21 +306,23 @@ int launch_recon_fast(const ReconParams& p, int64_t npb, bool comp, cudaStream_t
 }
 
 __global__ void recon_reduce_kernel(const float2* __restrict__ part, int nsplit, int64_t J, float norm,
-                                    float2* out) {
-  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= J) return;
-  float sr = 0.f, si = 0.f;
+                                    const int32_t* perm, float2* out) {
+  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= J) return;
+  double sr = 0.0, si = 0.0;
   for (int s = 0; s < nsplit; ++s) {
-    const float2 v = part[(int64_t)s * J + j];
+    const float2 v = part[(int64_t)s * J + pos];
     sr += v.x;
     si += v.y;
   }
-  out[j] = make_float2(-sr * norm, -si * norm);
+  const int64_t j = perm ? (int64_t)perm[pos] : pos;
+  out[j] = make_float2((float)(-sr * norm), (float)(-si * norm));
 }
 
-int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, float2* out, cudaStream_t st) {
+int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, const int32_t* perm, float2* out,
+                        cudaStream_t st) {
   if (J <= 0) return VISS_OK;
-  recon_reduce_kernel<<<(unsigned)((J + 255) / 256), 256, 0, st>>>(partial, nsplit, J, norm, out);
+  recon_reduce_kernel<<<(unsigned)((J + 255) / 256), 256, 0, st>>>(partial, nsplit, J, norm, perm, out);
   VISS_LAUNCH_CHECK("recon_reduce_kernel");
   return VISS_OK;
 }
@@ -286,6 +339,7 @@ struct PlainRecArgs {
   const int32_t* snap;
   const int32_t* pair;
   const float* sat_pos;
+  const float4* satdir;
   int64_t K, J;
   int nsat;
   int rmask;
@@ -311,9 +365,9 @@ __global__ void recon_plain_kernel(const PlainRecArgs a) {
       if (fabsf(t0 - thetaP) < t0 && fabsf(p0 - phiP) < p0) continue;
     } else if (a.rmask == VISS_RECON_MASK_GEOMETRIC) {
       const int s = a.snap[k], pr = a.pair[k];
-      const float* q1 = a.sat_pos + ((int64_t)s * a.nsat + (pr & 0xffff)) * 3;
-      const float* q2 = a.sat_pos + ((int64_t)s * a.nsat + ((pr >> 16) & 0xffff)) * 3;
-      if (geo_occluded_exact(a.l[j], a.m[j], a.n[j], q1, a.R) || geo_occluded_exact(a.l[j], a.m[j], a.n[j], q2, a.R))
+      const int64_t g1 = (int64_t)s * a.nsat + (pr & 0xffff), g2 = (int64_t)s * a.nsat + ((pr >> 16) & 0xffff);
+      if (geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g1], a.sat_pos + 3 * g1, a.R) ||
+          geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g2], a.sat_pos + 3 * g2, a.R))
         continue;
     }
     const float ph = a.u[k] * lj / a.dl + a.v[k] * mj / a.dm + a.w[k] * nj / a.dn;
@@ -328,9 +382,10 @@ __global__ void recon_plain_kernel(const PlainRecArgs a) {
 }
 
 int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                       const viss_geometry* geo, const float* V, const float* ratios, const float* dlmn,
-                       float2* out, cudaStream_t st) {
+                       const viss_geometry* geo, const float* V, const float* ratios, const float4* satdir,
+                       const float* dlmn, float2* out, cudaStream_t st) {
   PlainRecArgs a{};
+  a.satdir = satdir;
   a.u = vis.u; a.v = vis.v; a.w = vis.w; a.wgt = vis.wgt; a.V = V;
   a.l = sky.l; a.m = sky.m; a.n = sky.n;
   a.r1 = ratios; a.r2 = ratios ? ratios + vis.K : nullptr;

@@ -21,6 +21,14 @@
 
 namespace viss {
 
+// s += x with the rounding error of the sum carried in c (Kahan).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 template <bool FRAC, bool COMP>
 __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const float4& lo, float c, int U,
                                          int V, int W, int FU, int FV, int FW, float UF, float VF, float WF,
@@ -110,7 +118,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   int U[VIS_TK], V[VIS_TK], W[VIS_TK];
   int FU[VIS_TK], FV[VIS_TK], FW[VIS_TK];
   float UF[VIS_TK], VF[VIS_TK], WF[VIS_TK];
-  float ar[VIS_TK], ai[VIS_TK];
+  float ar[VIS_TK], ai[VIS_TK];   // running totals (Kahan)
+  float cr[VIS_TK], ci[VIS_TK];   // their compensation
+  float tr[VIS_TK], ti[VIS_TK];   // this tile's sums
   bool any_win = false;
 #pragma unroll
   for (int i = 0; i < VIS_TK; ++i) {
@@ -132,7 +142,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
       sm.win[tid + i * VIS_THREADS] = wv;
       any_win |= wv.x <= wv.y && wv.z + 1 < wv.w;
     }
-    ar[i] = 0.f; ai[i] = 0.f;
+    ar[i] = ai[i] = cr[i] = ci[i] = 0.f;
   }
   float4 cone0 = make_float4(0.f, 0.f, 0.f, 2.f), cone1 = make_float4(-2.f, 0.f, 0.f, 0.f);
   if (GEO) {
@@ -148,6 +158,8 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   for (int64_t tile = jb; tile < je; tile += VIS_P) {
     const int np = (int)((je - tile) < VIS_P ? (je - tile) : VIS_P);
     __syncthreads();  // previous tile fully consumed
+#pragma unroll
+    for (int i = 0; i < VIS_TK; ++i) tr[i] = ti[i] = 0.f;
     int nfast = np, nmix = 0;
     bool masked_tile = false;
     if (GEO) {
@@ -242,7 +254,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i)
           vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
-                               ar[i], ai[i]);
+                               tr[i], ti[i]);
       }
     } else if (REF) {
       for (int pi = 0; pi < np; ++pi) {
@@ -257,17 +269,20 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         for (int i = 0; i < VIS_TK; ++i) {
           const float c = ref_hit(sm.win[tid + i * VIS_THREADS], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
           vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
-                               ar[i], ai[i]);
+                               tr[i], ti[i]);
         }
       }
     }
     if (GEO && nmix > 0) {
       int gm[VIS_TK], gn[VIS_TK];
+      float4 dm[VIS_TK], dn[VIS_TK];
 #pragma unroll
       for (int i = 0; i < VIS_TK; ++i) {
         const int64_t k = row0 + tid + i * VIS_THREADS;
         gm[i] = __ldg(&p.rows0[k].w);
         gn[i] = __ldg(&p.rows1[k].w);
+        dm[i] = __ldg(p.satdir + gm[i]);
+        dn[i] = __ldg(p.satdir + gn[i]);
       }
       for (int mi = 0; mi < nmix; ++mi) {
         const int pi = VIS_P - 1 - mi;
@@ -280,15 +295,18 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         const float c0 = __int_as_float(a.w);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const float4 dm = __ldg(p.satdir + gm[i]);
-          const float4 dn = __ldg(p.satdir + gn[i]);
-          const bool occ = geo_test(g, dm, gm[i], p) || geo_test(g, dn, gn[i], p);
+          const bool occ = geo_test(g, dm[i], gm[i], p) || geo_test(g, dn[i], gn[i], p);
           const float c = occ ? occ_val : c0;
           if (c != 0.f)
             vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
-                                 ar[i], ai[i]);
+                                 tr[i], ti[i]);
         }
       }
+    }
+#pragma unroll
+    for (int i = 0; i < VIS_TK; ++i) {
+      kahan_add(ar[i], cr[i], tr[i]);
+      kahan_add(ai[i], ci[i], ti[i]);
     }
   }
 
@@ -335,13 +353,13 @@ int launch_vis_fast(const VisParams& p, int64_t nrb, bool comp, cudaStream_t st)
 __global__ void vis_reduce_kernel(const float2* __restrict__ part, int nsplit, int64_t K, float2* out) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= K) return;
-  float sr = 0.f, si = 0.f;
+  double sr = 0.0, si = 0.0;
   for (int s = 0; s < nsplit; ++s) {
     const float2 v = part[(int64_t)s * K + k];
     sr += v.x;
     si += v.y;
   }
-  out[k] = make_float2(-sr, si);
+  out[k] = make_float2((float)-sr, (float)si);
 }
 
 int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st) {
@@ -363,6 +381,7 @@ struct PlainVisArgs {
   const int32_t* snap;
   const int32_t* pair;
   const float* sat_pos;
+  const float4* satdir;
   int64_t K, J;
   int nsat;
   int mask;
@@ -375,13 +394,6 @@ struct PlainVisArgs {
   float2* out;
 };
 
-__device__ bool plain_geo(const PlainVisArgs& a, int64_t k, int64_t j) {
-  const int s = a.snap[k], pr = a.pair[k];
-  const float* p1 = a.sat_pos + ((int64_t)s * a.nsat + (pr & 0xffff)) * 3;
-  const float* p2 = a.sat_pos + ((int64_t)s * a.nsat + ((pr >> 16) & 0xffff)) * 3;
-  return geo_occluded_exact(a.l[j], a.m[j], a.n[j], p1, a.R) || geo_occluded_exact(a.l[j], a.m[j], a.n[j], p2, a.R);
-}
-
 __global__ void vis_plain_kernel(const PlainVisArgs a) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K) return;
@@ -392,6 +404,15 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
     if (a.mask == VISS_MASK_REF_QUIRK) { if (M3 <= 0 && M4 >= 0) wv = make_int4(0, M4, M1, M2); }
     else if (M3 <= M4) wv = make_int4(M3, M4, M1, M2);
   }
+  const bool geo = a.mask == VISS_MASK_GEOMETRIC;
+  float4 d1 = make_float4(0.f, 0.f, 0.f, 0.f), d2 = d1;
+  const float *p1 = nullptr, *p2 = nullptr;
+  if (geo) {
+    const int s = a.snap[k], pr = a.pair[k];
+    const int64_t g1 = (int64_t)s * a.nsat + (pr & 0xffff), g2 = (int64_t)s * a.nsat + ((pr >> 16) & 0xffff);
+    d1 = a.satdir[g1]; d2 = a.satdir[g2];
+    p1 = a.sat_pos + 3 * g1; p2 = a.sat_pos + 3 * g2;
+  }
   const float m2pi = -2.0f * (float)kPi;
   float ar = 0.f, ai = 0.f;
   for (int64_t j = 0; j < a.J; ++j) {
@@ -400,8 +421,9 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
     if (wv.x <= wv.y) {
       const int64_t q = j / a.res, r = j % a.res;
       if (ref_hit(wv, (int)q, (int)r, j, a.res)) c = a.occ;
-    } else if (a.mask == VISS_MASK_GEOMETRIC && plain_geo(a, k, j)) {
-      c = a.occ;
+    } else if (geo) {
+      const float sx = a.l[j], sy = a.m[j], sz = a.n[j];
+      if (geo_test_plain(sx, sy, sz, d1, p1, a.R) || geo_test_plain(sx, sy, sz, d2, p2, a.R)) c = a.occ;
     }
     const float ph = uk * a.l[j] / a.dl + vk * a.m[j] / a.dm + wk * (a.n[j] - 1.0f) / a.dn;
     float sn, cs;
@@ -415,8 +437,9 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
 }
 
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                     const viss_geometry* geo, const float* dlmn, float2* out, cudaStream_t st) {
+                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st) {
   PlainVisArgs a{};
+  a.satdir = satdir;
   a.u = vis.u; a.v = vis.v; a.w = vis.w;
   a.l = sky.l; a.m = sky.m; a.n = sky.n; a.bright = sky.bright;
   a.shade = vis.shade; a.snap = vis.snap; a.pair = vis.pair;

@@ -110,6 +110,7 @@ __device__ __forceinline__ bool geo_occluded_exact(float sx_, float sy_, float s
 
 // -------------------------------------------------------- kernel params
 struct PixPrepArgs {
+  const int32_t* perm;  // position -> pixel (NULL: identity)
   const float* l;
   const float* m;
   const float* n;
@@ -192,7 +193,8 @@ struct ReconParams {
   const float* n;
   const float* sat_pos;
   const int* flags;
-  float2* out;            // partial [nsplit][J] or final
+  const int32_t* perm;    // position -> pixel (NULL: identity)
+  float2* out;            // partial [nsplit][J] by position, or final F by pixel
   int64_t K, J;
   int64_t kchunk;
   int nsplit;
@@ -205,6 +207,13 @@ struct ReconParams {
 
 // ------------------------------------------------------------- launchers
 int launch_prep_pixels(const PixPrepArgs& a, cudaStream_t st);
+int launch_pixel_keys(const float* l, const float* m, const float* n, int64_t J, uint32_t* keys, int32_t* idx,
+                      cudaStream_t st);
+// Spatial permutation of the sky (keys, then a stable radix sort); scratch from
+// the caller's workspace.  perm[pos] = pixel.
+size_t pixel_order_scratch(int64_t J);
+int pixel_order(const float* l, const float* m, const float* n, int64_t J, void* scratch, size_t scratch_bytes,
+                int32_t* perm, cudaStream_t st);
 int launch_prep_rows(const RowPrepArgs& a, bool recon, cudaStream_t st);
 int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satdir, cudaStream_t st);
 int launch_prep_rowblock_cones(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
@@ -214,14 +223,25 @@ int launch_prep_snapshot_cones(const float4* satdir, int64_t S, int nsat, float4
 int launch_vis_fast(const VisParams& p, int64_t nrb, bool compensated, cudaStream_t st);
 int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st);
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                     const viss_geometry* geo, const float* dlmn, float2* out, cudaStream_t st);
+                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st);
 
 int launch_recon_fast(const ReconParams& p, int64_t npb, bool compensated, cudaStream_t st);
-int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, float2* out,
+int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, const int32_t* perm, float2* out,
                         cudaStream_t st);
 int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                       const viss_geometry* geo, const float* V, const float* ratios, const float* dlmn,
-                       float2* out, cudaStream_t st);
+                       const viss_geometry* geo, const float* V, const float* ratios, const float4* satdir,
+                       const float* dlmn, float2* out, cudaStream_t st);
+
+// Fast geometric test of direction s (need not be unit) against satellite
+// direction d = {p_hat, cos alpha}: s_hat.p_hat + cos(alpha) < 0, decided in
+// double (from the original inputs) within GEO_EPS of the limb.
+__device__ __forceinline__ bool geo_test_plain(float sx, float sy, float sz, const float4& d, const float* pos,
+                                               double R) {
+  const float inv = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
+  const float e = fmaf(sx * inv, d.x, fmaf(sy * inv, d.y, fmaf(sz * inv, d.z, d.w)));
+  if (fabsf(e) >= 4.0f * GEO_EPS) return e < 0.f;
+  return geo_occluded_exact(sx, sy, sz, pos, R);
+}
 
 int device_sm_count();
 
