@@ -1,0 +1,86 @@
+"""Adjoint / autograd: the gradient of a visibility loss through the CUDA
+forward (viss_vis_dft) and adjoint (viss_recon) agrees with central finite
+differences on 64 random pixels and with the FP64 oracle gradient; a sky +
+per-baseline-gain fit reduces the loss (differentiable imaging at 10 MHz,
+28 baselines x 16,384 snapshots, 49,152 pixels, SNR 20)."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def setup():
+    import viss_recon_shade_gb300 as V
+    from viss_recon_shade_gb300.synth import WORKLOADS, make_sky, make_uvw
+    wl = WORKLOADS["cfg4_10MHz"]
+    d = make_uvw(wl)
+    l, m, n, b = make_sky(wl)
+    t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    d.update(l=t(l), m=t(m), n=t(n), truth=t(b / b.max()))
+    cfg = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=0.0)
+    return V, wl, d, cfg
+
+
+def forward(V, d, cfg, x):
+    from viss_recon_shade_gb300.autograd import vis_dft_autograd
+    return vis_dft_autograd(x, cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["snap"], d["pair"], d["sat_pos"])
+
+
+def test_gradient_vs_finite_differences_and_fp64(setup, oracle):
+    V, wl, d, cfg = setup
+    J = d["l"].numel()
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    Vt = forward(V, d, cfg, d["truth"])
+    noise = (torch.randn(Vt.shape, generator=gen, device="cuda") + 1j * torch.randn(Vt.shape, generator=gen,
+                                                                                        device="cuda")) / np.sqrt(2)
+    V_obs = (Vt + noise.to(torch.complex64) * Vt.abs().mean() / 20).detach()
+    x0 = (d["truth"] * 0.5 + 0.1).requires_grad_(True)
+    loss = ((forward(V, d, cfg, x0) - V_obs).abs() ** 2).sum()
+    loss.backward()
+    grad = x0.grad.double().cpu().numpy()
+
+    # FP64 oracle gradient: 2 Re(A^H r), r = A x0 - V_obs
+    h = lambda t: t.detach().cpu().numpy()  # noqa: E731
+    r = h(forward(V, d, cfg, x0.detach()) - V_obs).astype(np.complex128)
+    K = r.size
+    oc = oracle.make_cfg(mask_mode=3, phase_scale=1.0, n_offset=-1.0, occluded_value=0.0, norm=1.0)
+    geo = oracle.make_geo(h(d["sat_pos"]), h(d["snap"]), h(d["pair"]))
+    pix = np.random.default_rng(1).choice(J, 64, replace=False)
+    g64 = 2 * oracle.recon(oc, h(d["u"]), h(d["v"]), h(d["w"]), None, r.astype(np.complex64), h(d["l"])[pix],
+                           h(d["m"])[pix], h(d["n"])[pix], geo=geo).real
+    e64 = np.linalg.norm(grad[pix] - g64) / np.linalg.norm(g64)
+    assert e64 < 1e-4, e64
+
+    # central finite differences on the same 64 pixels (the loss is quadratic in x,
+    # so the only error is float rounding of the forward passes)
+    x = x0.detach()
+    fd = np.zeros(64)
+    step = 0.05
+    for i, j in enumerate(pix):
+        e = torch.zeros_like(x)
+        e[j] = step
+        lp = ((forward(V, d, cfg, x + e) - V_obs).abs().double() ** 2).sum().item()
+        lm = ((forward(V, d, cfg, x - e) - V_obs).abs().double() ** 2).sum().item()
+        fd[i] = (lp - lm) / (2 * step)
+    efd = np.linalg.norm(grad[pix] - fd) / np.linalg.norm(fd)
+    assert efd < 1e-4, efd
+
+
+def test_fit_sky_and_gains_reduces_loss(setup):
+    V, wl, d, cfg = setup
+    from viss_recon_shade_gb300.autograd import fit_sky_and_gains
+    gen = torch.Generator(device="cuda").manual_seed(2)
+    nb = wl.npairs
+    true_g = (1 + 0.05 * torch.randn(nb, generator=gen, device="cuda")) * torch.exp(
+        1j * 0.05 * torch.randn(nb, generator=gen, device="cuda"))
+    baseline = torch.arange(d["u"].numel(), device="cuda") % nb
+    Vt = forward(V, d, cfg, d["truth"]).detach() * true_g.to(torch.complex64)[baseline]
+    noise = (torch.randn(Vt.shape, generator=gen, device="cuda") + 1j * torch.randn(Vt.shape, generator=gen,
+                                                                                        device="cuda")) / np.sqrt(2)
+    V_obs = Vt + noise.to(torch.complex64) * Vt.abs().mean() / 20
+    res = fit_sky_and_gains(V_obs, cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["snap"], d["pair"],
+                            d["sat_pos"], baseline, nb, steps=100)
+    assert res.losses[-1] < 0.2 * res.losses[0]
+    assert torch.all(res.sky >= 0)

@@ -81,7 +81,29 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
         cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
         run(cmd)
         os.replace(tmp, LIB)
+    build_tools(run, force)
     return LIB
+
+
+# Drop-in programs with the reference's names (one binary, dispatched on argv[0]).
+TOOL_NAMES = ["vissGen10M_shade", "vissGen10M_shade_optim1", "vissGen10M_shade_optim2", "vissGen1M_shade_optim1",
+              "vissGen1M_shade_optim2", "shade1M", "shade10M", "shade30M", "MIncline_generate_uvw_float"]
+
+
+def build_tools(run, force=False):
+    src = CSRC / "dropin.cpp"
+    bindir = OUT / "bin"
+    bindir.mkdir(exist_ok=True)
+    exe = bindir / "viss_dropin"
+    if force or _newer(exe, [src, LIB, INCLUDE / "viss_gb300.h"]):
+        tmp = bindir / f"viss_dropin.{os.getpid()}.tmp"
+        run([nvcc(), "-x", "c++", "-O2", "-std=c++17", f"-I{INCLUDE}", str(src), "-o", str(tmp), f"-L{OUT}",
+             "-lvissgb", "-lcudart", "-Xlinker", "-rpath", "-Xlinker", "$ORIGIN/.."])
+        os.replace(tmp, exe)
+    for name in TOOL_NAMES:
+        link = bindir / name
+        if not link.exists():
+            link.symlink_to("viss_dropin")
 
 
 if __name__ == "__main__":
