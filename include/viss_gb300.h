@@ -130,6 +130,21 @@ VISS_API int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const vi
                  const viss_geometry* geo, float* V, void* workspace, size_t workspace_bytes,
                  void* stream);
 
+/* Shaded visibility DFT without any allocation (no counterpart in the reference).
+ * For callers that must not have a library allocate device memory -- hosts
+ * that own a fixed memory budget or pool, or latency-bound loops that cannot
+ * take cudaMalloc's synchronisation -- and that do not want to pass a
+ * workspace either.  Same arguments and result as viss_vis_dft; the scratch is
+ * a VISS_NOALLOC_SCRATCH_BYTES array inside the library, resident on every GPU
+ * that loads it.  Passes whose viss_vis_dft_workspace() exceeds that size are
+ * rejected with VISS_ERR_RANGE (131,072 visibilities x 196,608 pixels with the
+ * geometric mask fit; the full 1,835,008 x 196,608 workload does not).  The first call on a device looks up the array's
+ * device address; make it before any stream capture.  Calls share the array:
+ * calls that overlap on the GPU race. */
+#define VISS_NOALLOC_SCRATCH_BYTES (32u << 20)
+VISS_API int viss_vis_dft_noalloc(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                                  const viss_geometry* geo, float* V, void* stream);
+
 /* Direct-DFT reconstruction (replaces imagerecon, vissGen10M_shade.cu:149-175,
  * and launch_imagerecon, vissGen10M_shade_optim2.cu:320-389).  V: K x 2, F: J x 2.
  * With norm = 1, wgt = NULL and the vis mask this is the adjoint of viss_vis_dft

@@ -65,6 +65,8 @@ _SIGS = {
     "viss_vis_dft_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.c_int64, C.c_int64, C.POINTER(Geometry)]),
     "viss_vis_dft": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Geometry), _P, _P,
                                C.c_size_t, _P]),
+    "viss_vis_dft_noalloc": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Geometry), _P,
+                                       _P]),
     "viss_recon_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.c_int64, C.c_int64, C.POINTER(Geometry)]),
     "viss_recon": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Geometry), _P, _P,
                              _P, C.c_size_t, _P]),
