@@ -81,8 +81,8 @@ static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, 
   p.nrb = p.Kpad / VIS_ROWS;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
   // Split the pixel axis when the visibility blocks alone fill less than
-  // ~4 waves of resident CTAs (3 per SM at 256 threads).
-  const int64_t slots = (int64_t)device_sm_count() * 3;
+  // ~4 waves of resident CTAs.
+  const int64_t slots = (int64_t)device_sm_count() * VISS_VIS_MINB;
   int64_t nsplit = 1;
   if (p.nrb < 4 * slots) nsplit = (4 * slots + p.nrb - 1) / p.nrb;
   const int64_t maxsplit = (J + VIS_P - 1) / VIS_P;
@@ -150,7 +150,7 @@ static void plan_recon(RecPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J
   p.npb = p.Jpad / REC_PIX;
   p.S = (geo && p.geo) ? geo->S : 0;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
-  const int64_t slots = (int64_t)device_sm_count() * 2;
+  const int64_t slots = (int64_t)device_sm_count() * VISS_REC_MINB;
   int64_t nsplit = 1;
   if (p.npb < 4 * slots) nsplit = (4 * slots + p.npb - 1) / p.npb;
   const int64_t maxsplit = (K + REC_Q - 1) / REC_Q;
@@ -182,6 +182,7 @@ static int check_geo(const viss_geometry* geo, const viss_vis_set* vis, const vi
   if (!geo || !geo->sat_pos) return fail(VISS_ERR_INVALID, "GEOMETRIC mask needs satellite positions");
   if (geo->nsat < 1 || geo->nsat > 32) return fail(VISS_ERR_RANGE, "nsat must be in [1, 32]");
   if (geo->S < 1) return fail(VISS_ERR_INVALID, "geometry has no snapshots");
+  if (geo->S * (int64_t)geo->nsat >= ((int64_t)1 << 26)) return fail(VISS_ERR_RANGE, "S * nsat must be < 2^26");
   if (!vis->snap || !vis->pair) return fail(VISS_ERR_INVALID, "GEOMETRIC mask needs snap and pair per visibility");
   if (!(cfg->moon_radius_km > 0.0)) return fail(VISS_ERR_RANGE, "moon_radius_km must be > 0");
   return VISS_OK;
@@ -241,6 +242,7 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   ra.u = vis.u; ra.v = vis.v; ra.w = vis.w; ra.shade = vis.shade;
   ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
   ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
+  ra.sn = scale[2]; ra.n_offset = cfg.n_offset;
   ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = cfg.mask_mode; ra.recon_mask = VISS_RECON_MASK_NONE;
   ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.flags = p.flags;
   if ((rc = launch_prep_rows(ra, false, st))) return rc;
@@ -310,6 +312,7 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   ra.shade = ratio_arrays ? nullptr : vis.shade;
   ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
   ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
+  ra.sn = scale[2]; ra.n_offset = cfg.n_offset;
   ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = VISS_MASK_NONE; ra.recon_mask = cfg.recon_mask;
   ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.y = p.y; ra.flags = p.flags;
   if ((rc = launch_prep_rows(ra, true, st))) return rc;

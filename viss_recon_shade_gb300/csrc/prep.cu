@@ -35,8 +35,9 @@ __global__ void prep_pixels_kernel(PixPrepArgs a) {
   const uint32_t A = fix32(x), B = fix32(y), C = fix32(z);
   a.rec0[pos] = make_int4((int)A, (int)B, (int)C, __float_as_int(b));
   if (a.rec1) {
-    a.rec1[pos] = make_int4((int)llrint(x * 1073741824.0), (int)llrint(y * 1073741824.0),
-                          (int)llrint(z * 1073741824.0), (int)j);
+    // coordinates for the fractional part of uvw; z without the n_offset shift (|s*n| <= 1)
+    a.rec1[pos] = make_int4(__float_as_int((float)x), __float_as_int((float)y),
+                            __float_as_int((float)(a.sn * (double)a.n[j])), (int)j);
   }
   if (a.lo) {
     const double sc = 4294967296.0;
@@ -61,12 +62,13 @@ __global__ void prep_pixels_kernel(PixPrepArgs a) {
 // on the face of the cube it points to and the face coordinates (10 bits each)
 // are interleaved (Morton), so consecutive positions are neighbouring pixels
 // and a warp's pixels see the Moon's limb together.
+// 10 bits -> the even bits of 20 (2-D Morton interleave)
 __device__ __forceinline__ uint32_t spread10(uint32_t x) {
   x &= 0x3ff;
-  x = (x | (x << 16)) & 0x030000ff;
-  x = (x | (x << 8)) & 0x0300f00f;
-  x = (x | (x << 4)) & 0x030c30c3;
-  x = (x | (x << 2)) & 0x09249249;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
   return x;
 }
 
@@ -127,7 +129,7 @@ __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
   if (k >= a.Kpad) return;
   if (k >= a.K) {
     a.rec0[k] = make_int4(0, 0, 0, 0);
-    a.rec1[k] = make_int4(0, 0, 0, 0);
+    a.rec1[k] = make_int4(0, 0, 0, PHASE_BIAS);
     if (a.uf) a.uf[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.win) a.win[k] = make_int4(1, 0, 0, 0);
     if (a.y) a.y[k] = make_float2(0.f, 0.f);
@@ -137,11 +139,9 @@ __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
   const double Uu = floor(uu + 0.5), Uv = floor(vv + 0.5), Uw = floor(ww + 0.5);
   const double lim = 1073741824.0;  // |U| < 2^30
   if (!(fabs(Uu) < lim && fabs(Uv) < lim && fabs(Uw) < lim)) atomicOr(a.flags + 1, 1);
-  const int Fu = (int)llrint((uu - Uu) * 4294967296.0);
-  const int Fv = (int)llrint((vv - Uv) * 4294967296.0);
-  const int Fw = (int)llrint((ww - Uw) * 4294967296.0);
-  if (Fu | Fv | Fw) atomicOr(a.flags, 1);
-  int gm = 0, gn = 0;
+  const double fu = uu - Uu, fv = vv - Uv, fw = ww - Uw;  // exact, in [-1/2, 1/2)
+  if (fu != 0.0 || fv != 0.0 || fw != 0.0) atomicOr(a.flags, 1);
+  int packed = 0;
   if (a.snap && a.pair) {
     const int s = a.snap[k];
     const int pr = a.pair[k];
@@ -149,12 +149,13 @@ __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
     if (s < 0 || s >= a.S || pm >= a.nsat || pn >= a.nsat) {
       atomicOr(a.flags + 1, 2);
     } else {
-      gm = s * a.nsat + pm;
-      gn = s * a.nsat + pn;
+      packed = (s * a.nsat + pm) | ((pn - pm + 32) << 26);
     }
   }
-  a.rec0[k] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, gm);
-  a.rec1[k] = make_int4(Fu, Fv, Fw, gn);
+  // PHASE_BIAS plus the per-row part of f_w * z: f_w * sn * n_offset
+  const int bias = (int)((uint32_t)PHASE_BIAS + fix32(fw * a.sn * a.n_offset));
+  a.rec0[k] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, packed);
+  a.rec1[k] = make_int4(__float_as_int((float)fu), __float_as_int((float)fv), __float_as_int((float)fw), bias);
   if (a.uf) a.uf[k] = make_float4((float)Uu, (float)Uv, (float)Uw, 0.f);
   if (a.win) {
     int4 wv = make_int4(1, 0, 0, 0);  // empty
@@ -310,8 +311,8 @@ struct RowMember {
   const int4* rows1;
   int64_t base;
   __device__ int operator()(int64_t i) const {
-    const int64_t k = base + (i >> 1);
-    return (i & 1) ? rows1[k].w : rows0[k].w;
+    const int p = rows0[base + (i >> 1)].w;
+    return (i & 1) ? sat_gn(p) : sat_gm(p);
   }
 };
 

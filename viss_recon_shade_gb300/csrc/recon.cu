@@ -27,17 +27,16 @@ __device__ __noinline__ bool geo_exact_pix(const ReconParams& p, int j, int gidx
 
 template <bool FRAC, bool COMP>
 __device__ __forceinline__ void rec_term(const int4& r0, const int4& r1, const float4& rf, float2 y, int A, int B,
-                                         int C, int Ap, int Bp, int Cp, float lx, float ly, float lz, float& fr,
+                                         int C, float X, float Y, float Z, float lx, float ly, float lz, float& fr,
                                          float& fi) {
   uint32_t q = (uint32_t)r0.x * (uint32_t)A + (uint32_t)r0.y * (uint32_t)B + (uint32_t)r0.z * (uint32_t)C +
-               (uint32_t)PHASE_BIAS;
-  if (FRAC) {
-    const uint32_t h = (uint32_t)mulhi(r1.x, Ap) + (uint32_t)mulhi(r1.y, Bp) + (uint32_t)mulhi(r1.z, Cp);
-    q += h << 2;
-  }
+               (uint32_t)(FRAC ? r1.w : PHASE_BIAS);
+  float delta = 0.f;
+  if (FRAC) delta = fmaf(__int_as_float(r1.x), X, fmaf(__int_as_float(r1.y), Y, __int_as_float(r1.z) * Z));
+  if (FRAC && !COMP) q += frac_phase(delta);
   float x = turns_to_angle(q);
   if (COMP) {
-    const float d = fmaf(rf.x, lx, fmaf(rf.y, ly, rf.z * lz));
+    const float d = fmaf(rf.x, lx, fmaf(rf.y, ly, fmaf(rf.z, lz, delta)));
     x = fmaf(d, K2PI, x);
   }
   float sn, cs;
@@ -64,15 +63,8 @@ struct RecSmem {
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
   float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
   int srange[2];
+  float4 acc[REC_PIX];            // running totals (re, im) and their Kahan compensation per pixel
 };
-
-// s += x with the rounding error of the sum carried in c (Kahan).
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-  const float y = x - c;
-  const float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
 
 template <int RM, bool FRAC, bool COMP>
 __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm) {
@@ -80,31 +72,26 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
   // a warp owns 32 * REC_TJ consecutive positions: with the spatial order of
   // the geometric passes that is one compact patch of sky
   const int64_t j0 = (int64_t)blockIdx.x * REC_PIX + (int64_t)tid * REC_TJ;
-  int A[REC_TJ], B[REC_TJ], C[REC_TJ], Ap[REC_TJ], Bp[REC_TJ], Cp[REC_TJ];
+  int A[REC_TJ], B[REC_TJ], C[REC_TJ];
+  float XF[REC_TJ], YF[REC_TJ], ZF[REC_TJ];
   float LX[REC_TJ], LY[REC_TJ], LZ[REC_TJ];
-  float GX[REC_TJ], GY[REC_TJ], GZ[REC_TJ];
-  int TP[REC_TJ], PP[REC_TJ], JJ[REC_TJ];
-  float fr[REC_TJ], fi[REC_TJ];    // running totals (Kahan)
-  float cr[REC_TJ], ci[REC_TJ];    // their compensation
+  int TP[REC_TJ], PP[REC_TJ];
+  // running totals live in sm.acc; pixel directions (geometric) are re-read per snapshot run
 #pragma unroll
   for (int i = 0; i < REC_TJ; ++i) {
     const int64_t pos = j0 + i;  // pixels padded to a whole block
     const int4 a = p.pix0[pos];
     A[i] = a.x; B[i] = a.y; C[i] = a.z;
-    Ap[i] = Bp[i] = Cp[i] = 0;
-    JJ[i] = (int)pos;
-    if (FRAC || RM == RM_GEO) {
+    XF[i] = YF[i] = ZF[i] = 0.f;
+    if (FRAC) {
       const int4 b = p.pix1[pos];
-      Ap[i] = b.x; Bp[i] = b.y; Cp[i] = b.z;
-      JJ[i] = b.w;  // original pixel index
+      XF[i] = __int_as_float(b.x); YF[i] = __int_as_float(b.y); ZF[i] = __int_as_float(b.z);
     }
     LX[i] = LY[i] = LZ[i] = 0.f;
     if (COMP) { const float4 lo = p.plo[pos]; LX[i] = lo.x; LY[i] = lo.y; LZ[i] = lo.z; }
-    GX[i] = GY[i] = GZ[i] = 0.f;
-    if (RM == RM_GEO) { const float4 g = p.pgeo[pos]; GX[i] = g.x; GY[i] = g.y; GZ[i] = g.z; }
     TP[i] = PP[i] = -1;
     if (RM == RM_REF) { const int2 qr = p.pqr[pos]; PP[i] = qr.x; TP[i] = qr.y; }
-    fr[i] = fi[i] = cr[i] = ci[i] = 0.f;
+    sm.acc[tid * REC_TJ + i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   bool valid[REC_TJ];
 #pragma unroll
@@ -126,7 +113,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
       const int64_t k = tile + r;
       const int4 r0 = p.rows0[k];
       sm.r0[r] = r0;
-      if (FRAC || RM == RM_GEO) sm.r1[r] = p.rows1[k];
+      if (FRAC) sm.r1[r] = p.rows1[k];
       if (COMP) sm.rf[r] = p.rowsf[k];
       sm.y[r] = p.y[k];
       if (RM == RM_REF) {
@@ -138,7 +125,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         }
       }
       if (RM == RM_GEO) {
-        const int sn = r0.w / p.nsat;
+        const int sn = sat_gm(r0.w) / p.nsat;
         sm.snap[r] = sn;
         atomicMin(&sm.srange[0], sn);
         atomicMax(&sm.srange[1], sn);
@@ -173,7 +160,8 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         bool all_vis = true, all_occ = true;
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i) {
-          const float d = fmaf(GX[i], c0.x, fmaf(GY[i], c0.y, GZ[i] * c0.z));
+          const float4 g = __ldg(p.pgeo + j0 + i);
+          const float d = fmaf(g.x, c0.x, fmaf(g.y, c0.y, g.z * c0.z));
           all_vis &= (!valid[i]) || d < c1;
           all_occ &= (!valid[i]) || d > c0.w;
         }
@@ -191,7 +179,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
             const float2 y = sm.y[rr];
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i)
-              rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
+              rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
                                    tr[i], ti[i]);
           }
         } else {
@@ -200,27 +188,29 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
           const int g0 = sn * p.nsat;
 #pragma unroll
           for (int i = 0; i < REC_TJ; ++i) bits[i] = 0u;
-          for (int sat = 0; sat < p.nsat; ++sat) {
-            const float4 d = cached ? sm.sat[(sn - s_lo) * p.nsat + sat] : __ldg(p.satdir + g0 + sat);
 #pragma unroll
-            for (int i = 0; i < REC_TJ; ++i) {
-              const float e = fmaf(GX[i], d.x, fmaf(GY[i], d.y, fmaf(GZ[i], d.z, d.w)));
+          for (int i = 0; i < REC_TJ; ++i) {
+            const float4 g = __ldg(p.pgeo + j0 + i);
+            for (int sat = 0; sat < p.nsat; ++sat) {
+              const float4 d = cached ? sm.sat[(sn - s_lo) * p.nsat + sat] : __ldg(p.satdir + g0 + sat);
+              const float e = fmaf(g.x, d.x, fmaf(g.y, d.y, fmaf(g.z, d.z, d.w)));
               bool occ = e < 0.f;
-              if (fabsf(e) < GEO_EPS && valid[i]) occ = geo_exact_pix(p, JJ[i], g0 + sat);
+              if (fabsf(e) < GEO_EPS && valid[i]) occ = geo_exact_pix(p, __float_as_int(g.w), g0 + sat);
               bits[i] |= (occ ? 1u : 0u) << sat;
             }
           }
           for (int rr = r; rr < re; ++rr) {
             const int4 r0 = sm.r0[rr];
-            const int4 r1 = sm.r1[rr];
+            int4 r1 = make_int4(0, 0, 0, 0);
+            if (FRAC) r1 = sm.r1[rr];
             float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
             if (COMP) rf = sm.rf[rr];
             const float2 y = sm.y[rr];
-            const uint32_t pm = (1u << (r0.w - g0)) | (1u << (r1.w - g0));
+            const uint32_t pm = (1u << (sat_gm(r0.w) - g0)) | (1u << (sat_gn(r0.w) - g0));
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i) {
               const float2 yy = (bits[i] & pm) ? make_float2(0.f, 0.f) : y;
-              rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i],
+              rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
                                    tr[i], ti[i]);
             }
           }
@@ -240,7 +230,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         for (int i = 0; i < REC_TJ; ++i) {
           const bool skip = TP[i] >= 1 && TP[i] <= wv.x && PP[i] >= 1 && PP[i] <= wv.y;
           const float2 yy = skip ? make_float2(0.f, 0.f) : y;
-          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], tr[i],
+          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
                                ti[i]);
         }
       }
@@ -255,33 +245,37 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         const float2 y = sm.y[rr];
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i)
-          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], Ap[i], Bp[i], Cp[i], LX[i], LY[i], LZ[i], tr[i],
+          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
                                ti[i]);
       }
     }
 #pragma unroll
     for (int i = 0; i < REC_TJ; ++i) {
-      kahan_add(fr[i], cr[i], tr[i]);
-      kahan_add(fi[i], ci[i], ti[i]);
+      float4 t = sm.acc[tid * REC_TJ + i];  // owned by this thread alone
+      kahan_add(t.x, t.z, tr[i]);
+      kahan_add(t.y, t.w, ti[i]);
+      sm.acc[tid * REC_TJ + i] = t;
     }
   }
   // F = norm * (-fr - i fi)  (the angle carried an extra half turn)
 #pragma unroll
   for (int i = 0; i < REC_TJ; ++i) {
     const int64_t pos = j0 + i;
+    const float4 t = sm.acc[tid * REC_TJ + i];
+    const float fr = t.x, fi = t.y;
     if (pos < p.J) {
       if (p.nsplit == 1) {
         const int64_t j = p.perm ? (int64_t)p.perm[pos] : pos;
-        p.out[j] = make_float2(-fr[i] * p.norm, -fi[i] * p.norm);
+        p.out[j] = make_float2(-fr * p.norm, -fi * p.norm);
       } else {
-        p.out[(int64_t)blockIdx.y * p.J + pos] = make_float2(fr[i], fi[i]);
+        p.out[(int64_t)blockIdx.y * p.J + pos] = make_float2(fr, fi);
       }
     }
   }
 }
 
 template <int RM, bool COMP>
-__global__ void __launch_bounds__(REC_THREADS, 2) recon_fast_kernel(const ReconParams p) {
+__global__ void __launch_bounds__(REC_THREADS, VISS_REC_MINB) recon_fast_kernel(const ReconParams p) {
   __shared__ RecSmem<RM, COMP> sm;
   if (__ldg(p.flags) != 0) recon_body<RM, true, COMP>(p, sm);
   else recon_body<RM, false, COMP>(p, sm);

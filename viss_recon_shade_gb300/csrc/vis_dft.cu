@@ -21,27 +21,19 @@
 
 namespace viss {
 
-// s += x with the rounding error of the sum carried in c (Kahan).
-__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-  const float y = x - c;
-  const float t = s + y;
-  c = (t - s) - y;
-  s = t;
-}
-
 template <bool FRAC, bool COMP>
 __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const float4& lo, float c, int U,
-                                         int V, int W, int FU, int FV, int FW, float UF, float VF, float WF,
-                                         float& ar, float& ai) {
+                                         int V, int W, float FU, float FV, float FW, int bias, float UF, float VF,
+                                         float WF, float& ar, float& ai) {
   uint32_t q = (uint32_t)U * (uint32_t)a.x + (uint32_t)V * (uint32_t)a.y + (uint32_t)W * (uint32_t)a.z +
-               (uint32_t)PHASE_BIAS;
-  if (FRAC) {
-    const uint32_t h = (uint32_t)mulhi(FU, b.x) + (uint32_t)mulhi(FV, b.y) + (uint32_t)mulhi(FW, b.z);
-    q += h << 2;
-  }
+               (uint32_t)(FRAC ? bias : PHASE_BIAS);
+  float delta = 0.f;
+  if (FRAC) delta = fmaf(FU, __int_as_float(b.x), fmaf(FV, __int_as_float(b.y), FW * __int_as_float(b.z)));
+  if (FRAC && !COMP) q += frac_phase(delta);
   float x = turns_to_angle(q);
   if (COMP) {
-    const float d = fmaf(UF, lo.x, fmaf(VF, lo.y, WF * lo.z));
+    // fractional part and the pixel fixed-point rounding, in FP32, added to the angle
+    const float d = fmaf(UF, lo.x, fmaf(VF, lo.y, fmaf(WF, lo.z, delta)));
     x = fmaf(d, K2PI, x);
   }
   float sn, cs;
@@ -95,6 +87,7 @@ struct VisSmem {
   int2 qr[REF ? VIS_P : 1];
   int4 win[REF ? VIS_ROWS : 1];   // the block's REF windows, read in masked tiles only
   int wcnt[VIS_THREADS / 32][2];
+  float4 acc[VIS_ROWS];           // running totals (re, im) and their Kahan compensation per visibility
 };
 
 template <int MASK, bool FRAC, bool COMP>
@@ -115,22 +108,21 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   // Registers per visibility: fixed-point U,V,W [+ fractional F] [+ float U for
   // the compensation] and the two accumulators.  Satellite indices (geometric)
   // and windows (REF) are fetched only on the masked paths.
-  int U[VIS_TK], V[VIS_TK], W[VIS_TK];
-  int FU[VIS_TK], FV[VIS_TK], FW[VIS_TK];
+  int U[VIS_TK], V[VIS_TK], W[VIS_TK], BI[VIS_TK];
+  float FU[VIS_TK], FV[VIS_TK], FW[VIS_TK];
   float UF[VIS_TK], VF[VIS_TK], WF[VIS_TK];
-  float ar[VIS_TK], ai[VIS_TK];   // running totals (Kahan)
-  float cr[VIS_TK], ci[VIS_TK];   // their compensation
-  float tr[VIS_TK], ti[VIS_TK];   // this tile's sums
+  float tr[VIS_TK], ti[VIS_TK];   // this tile's sums; running totals live in sm.acc
   bool any_win = false;
 #pragma unroll
   for (int i = 0; i < VIS_TK; ++i) {
     const int64_t k = row0 + tid + i * VIS_THREADS;  // rows are padded to a whole block
     const int4 r0 = p.rows0[k];
     U[i] = r0.x; V[i] = r0.y; W[i] = r0.z;
-    FU[i] = FV[i] = FW[i] = 0;
+    FU[i] = FV[i] = FW[i] = 0.f;
+    BI[i] = PHASE_BIAS;
     if (FRAC) {
       const int4 r1 = p.rows1[k];
-      FU[i] = r1.x; FV[i] = r1.y; FW[i] = r1.z;
+      FU[i] = __int_as_float(r1.x); FV[i] = __int_as_float(r1.y); FW[i] = __int_as_float(r1.z); BI[i] = r1.w;
     }
     UF[i] = VF[i] = WF[i] = 0.f;
     if (COMP) {
@@ -142,7 +134,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
       sm.win[tid + i * VIS_THREADS] = wv;
       any_win |= wv.x <= wv.y && wv.z + 1 < wv.w;
     }
-    ar[i] = ai[i] = cr[i] = ci[i] = 0.f;
+    sm.acc[tid + i * VIS_THREADS] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   float4 cone0 = make_float4(0.f, 0.f, 0.f, 2.f), cone1 = make_float4(-2.f, 0.f, 0.f, 0.f);
   if (GEO) {
@@ -253,7 +245,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         const float c = __int_as_float(a.w);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i)
-          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
                                tr[i], ti[i]);
       }
     } else if (REF) {
@@ -268,21 +260,19 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
           const float c = ref_hit(sm.win[tid + i * VIS_THREADS], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
-          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+          vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
                                tr[i], ti[i]);
         }
       }
     }
     if (GEO && nmix > 0) {
       int gm[VIS_TK], gn[VIS_TK];
-      float4 dm[VIS_TK], dn[VIS_TK];
 #pragma unroll
       for (int i = 0; i < VIS_TK; ++i) {
         const int64_t k = row0 + tid + i * VIS_THREADS;
-        gm[i] = __ldg(&p.rows0[k].w);
-        gn[i] = __ldg(&p.rows1[k].w);
-        dm[i] = __ldg(p.satdir + gm[i]);
-        dn[i] = __ldg(p.satdir + gn[i]);
+        const int pk = __ldg(&p.rows0[k].w);
+        gm[i] = sat_gm(pk);
+        gn[i] = sat_gn(pk);
       }
       for (int mi = 0; mi < nmix; ++mi) {
         const int pi = VIS_P - 1 - mi;
@@ -295,18 +285,21 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         const float c0 = __int_as_float(a.w);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const bool occ = geo_test(g, dm[i], gm[i], p) || geo_test(g, dn[i], gn[i], p);
+          // the rows' satellite directions stay in L1 for the whole mixed list
+          const bool occ = geo_test(g, __ldg(p.satdir + gm[i]), gm[i], p) || geo_test(g, __ldg(p.satdir + gn[i]), gn[i], p);
           const float c = occ ? occ_val : c0;
           if (c != 0.f)
-            vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], UF[i], VF[i], WF[i],
+            vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
                                  tr[i], ti[i]);
         }
       }
     }
 #pragma unroll
     for (int i = 0; i < VIS_TK; ++i) {
-      kahan_add(ar[i], cr[i], tr[i]);
-      kahan_add(ai[i], ci[i], ti[i]);
+      float4 t = sm.acc[tid + i * VIS_THREADS];  // owned by this thread alone
+      kahan_add(t.x, t.z, tr[i]);
+      kahan_add(t.y, t.w, ti[i]);
+      sm.acc[tid + i * VIS_THREADS] = t;
     }
   }
 
@@ -314,18 +307,17 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 #pragma unroll
   for (int i = 0; i < VIS_TK; ++i) {
     const int64_t k = row0 + tid + i * VIS_THREADS;
+    const float4 t = sm.acc[tid + i * VIS_THREADS];
+    const float ar = t.x, ai = t.y;
     if (k < p.K) {
-      if (p.nsplit == 1) p.out[k] = make_float2(-ar[i], ai[i]);
-      else p.out[(int64_t)split * p.K + k] = make_float2(ar[i], ai[i]);
+      if (p.nsplit == 1) p.out[k] = make_float2(-ar, ai);
+      else p.out[(int64_t)split * p.K + k] = make_float2(ar, ai);
     }
   }
 }
 
-// Integer-valued uvw (the reference's ceil(), MIncline:156-158) need no
-// fractional term; the row prep sets flags[0] when any uvw is fractional and
-// the kernel picks its loop from that flag (uniform branch, no host sync).
 template <int MASK, bool COMP>
-__global__ void __launch_bounds__(VIS_THREADS, 2) vis_fast_kernel(const VisParams p) {
+__global__ void __launch_bounds__(VIS_THREADS, VISS_VIS_MINB) vis_fast_kernel(const VisParams p) {
   __shared__ VisSmem<MASK, COMP> sm;
   if (__ldg(p.flags) != 0) vis_body<MASK, true, COMP>(p, sm);
   else vis_body<MASK, false, COMP>(p, sm);

@@ -69,6 +69,15 @@ constexpr int REC_TJ = 4;                 // pixels per thread
 constexpr int REC_PIX = REC_THREADS * REC_TJ;
 constexpr int REC_Q = 256;                // visibilities per shared-memory tile
 
+// Resident CTAs per SM the tiled kernels are compiled for (register budget
+// 65536 / (256 * n)).
+#ifndef VISS_VIS_MINB
+#define VISS_VIS_MINB 3
+#endif
+#ifndef VISS_REC_MINB
+#define VISS_REC_MINB 3
+#endif
+
 // Geometric test: |e| below this margin is re-decided in double.
 constexpr float GEO_EPS = 2e-6f;
 
@@ -79,9 +88,12 @@ enum PixClass : int { CLS_VIS = 0, CLS_OCC = 1, CLS_MIX = 2 };
 //   A  = round(x * 2^32) mod 2^32  -- the integer part of u multiplies it exactly mod 1 turn
 //   A' = round(x * 2^30)           -- for the fractional part of u (|x| < 2)
 //   lo = x - A*2^-32 (float)       -- compensation of the rounding of A
-// A visibility coordinate u is split u = U + f, U = floor(u + 1/2), f in [-1/2, 1/2),
-// F = f * 2^32 (exact for |u| >= 1/2).
-// Phase (turns * 2^32, mod 2^32) = U*A + ((F*A') >> 32) * 4.
+// A visibility coordinate u is split u = U + f, U = floor(u + 1/2), f in [-1/2, 1/2).
+// Phase (turns * 2^32, mod 2^32) = U*A + V*B + W*C + bias_k + frac, where the
+// fractional part delta = f_u*x + f_v*y + f_w*z' (FP32, |delta| < 2, z' = s*n) is
+// folded in with one FADD: the bits of (delta + 6.0f) hold delta in units of
+// 2^-21 turns above the constant 0x40C00000, whose shift by 11 vanishes mod 2^32,
+// so frac = bits(delta + 6) << 11.  bias_k carries f_w*s*n_offset.
 __device__ __forceinline__ uint32_t fix32(double x) {
   return (uint32_t)(unsigned long long)llrint(x * 4294967296.0);
 }
@@ -93,7 +105,23 @@ __device__ __forceinline__ float turns_to_angle(uint32_t q) {
   return fmaf(f, K2PI, KM3PI);
 }
 
-__device__ __forceinline__ int mulhi(int a, int b) { return __mulhi(a, b); }
+// delta (turns, |delta| < 2) -> its fixed-point phase contribution (units 2^-32, resolution 2^-21)
+__device__ __forceinline__ uint32_t frac_phase(float delta) {
+  return __float_as_uint(delta + 6.0f) << 11;
+}
+
+// Satellite indices of a visibility (geometric mask): gm = snapshot*nsat + m in the
+// low 26 bits, n - m + 32 in the top 6.
+__device__ __forceinline__ int sat_gm(int packed) { return packed & 0x3ffffff; }
+__device__ __forceinline__ int sat_gn(int packed) { return (packed & 0x3ffffff) + (int)((uint32_t)packed >> 26) - 32; }
+
+// s += x with the rounding error of the sum carried in c (Kahan).
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = x - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
 
 // Exact geometric predicate in double, same operation order as the oracle.
 __device__ __forceinline__ bool geo_occluded_exact(float sx_, float sy_, float sz_, const float* p,
@@ -120,13 +148,14 @@ struct PixPrepArgs {
   int res;
   int trunc;
   int4* rec0;     // {A, B, C, bright bits}
-  int4* rec1;     // {A', B', C', j}
+  int4* rec1;     // {x, y, s*n (float bits), j}
   float4* lo;     // {a_lo, b_lo, c_lo, 0}
   float4* geo;    // {unit s, j bits}
   int2* qr;       // {j / res, j % res}
 };
 
 struct RowPrepArgs {
+  double sn, n_offset;   // z = sn * (n + n_offset): the f_w * sn * n_offset part goes to the row bias
   const float* u;
   const float* v;
   const float* w;
@@ -140,8 +169,8 @@ struct RowPrepArgs {
   int64_t K, Kpad;
   int mask_mode;
   int recon_mask;
-  int4* rec0;   // {U, V, W, gm}
-  int4* rec1;   // {Fu, Fv, Fw, gn}
+  int4* rec0;   // {U, V, W, packed satellite indices}
+  int4* rec1;   // {f_u, f_v, f_w (float bits), phase bias}
   float4* uf;   // {U, V, W as float, 0}   (compensation)
   int4* win;    // vis REF: {lo_a, lo_b, M1, M2}; recon REF: {tmax, pmax, 0, 0}
   float2* y;    // recon: wgt * V
