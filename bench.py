@@ -156,8 +156,10 @@ def choose_precision(d, pref):
     if pref == "comp":
         return V.PREC_COMPENSATED
     umax = max(float(d[k].abs().max()) for k in ("u", "v", "w"))
-    # the fast path's phase error grows as |uvw| * 2^-33 turns per coordinate
-    return V.PREC_FAST if umax <= 4096 else V.PREC_COMPENSATED
+    # the fast path's phase error grows as |uvw| * 2^-33 turns per coordinate; up to
+    # |uvw| ~ 1.2e4 (30 MHz, 100 km baselines) it measures <= 1e-5 against FP64
+    # (tests/test_gpu_precision.py), beyond that the compensated path is needed
+    return V.PREC_FAST if umax <= 12000 else V.PREC_COMPENSATED
 
 
 def run_ours(args, ws, rank, local):
@@ -448,11 +450,146 @@ def ref_cuda_plain(wl, d):
         return {"unavailable": f"{type(e).__name__}: {e}"}
 
 
+# ------------------------------------------------------------------ batched channels
+def run_batch(args, ws, rank, local):
+    """--workload batch64: 64 channels log-spaced over 1-30 MHz, 28 baselines x
+    U[4096, 65536] snapshots each, 49,152 pixels with per-channel power-law
+    brightness, geometric mask; one persistent vis launch + one persistent recon
+    launch per step, replayed from a CUDA graph, launch parameters from the
+    autotuner (timed on every 8th channel).  Compared with the reference's form:
+    per-channel plain launches, timed on 4 channels spread over the band."""
+    import numpy as np
+    import torch
+    import viss_recon_shade_gb300 as V
+    from viss_recon_shade_gb300 import _lib as L
+    from viss_recon_shade_gb300.synth import BATCH_WORKLOADS, make_batch
+    bw = BATCH_WORKLOADS[args.workload]
+    d = make_batch(bw)
+    t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
+    lg, mg, ng = t(d["l"]), t(d["m"]), t(d["n"])
+    prec = choose_precision(d, args.precision)
+    cfg = V.DftConfig.north_star(precision=prec, occluded_value=0.0)
+    ro = d["row_off"]
+    K, J, nch = int(ro[-1]), bw.J, bw.nch
+
+    def make(chans, c=cfg):
+        r = np.concatenate([[0], np.cumsum([ro[i + 1] - ro[i] for i in chans])]).astype(np.int64)
+        if list(chans) == list(range(nch)):
+            sel = slice(None)
+            bright = d["bright"]
+        else:
+            idx = torch.cat([torch.arange(int(ro[i]), int(ro[i + 1]), device="cuda") for i in chans])
+            sel = idx
+            bright = d["bright"][list(chans)].contiguous()
+        return V.ChannelBatch(c, d["u"][sel], d["v"][sel], d["w"][sel], r, lg, mg, ng, bright, snap=d["snap"][sel],
+                              pair=d["pair"][sel], sat_pos=d["sat_pos"])
+
+    sub = make(list(range(0, nch, 8)))
+    best = V.autotune(sub, use_cache=False)
+    report = [{"tuning": vars(tn), "ms": round(ms, 2)} for tn, ms in V.autotune_report(sub)]
+    del sub
+    b = make(list(range(nch)))
+    b.set_tuning(best)
+    g = b.graph()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0e.record(st)
+        for _ in range(args.steps):
+            flush.zero_()
+            g.replay()
+        t1e.record(st)
+        torch.cuda.synchronize()
+        barrier(ws)
+    total_ms = max_over_ranks(t0e.elapsed_time(t1e), ws)
+    terms_step = 2.0 * K * J
+    value = terms_step * args.steps * ws / (total_ms * 1e-3) / 1e9
+    # split of one eager step
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    n0 = L.lib.viss_launch_count()
+    e0.record(st)
+    b.vis()
+    e1.record(st)
+    b.recon()
+    e2.record(st)
+    torch.cuda.synchronize()
+    vis_ms, rec_ms = e0.elapsed_time(e1), e1.elapsed_time(e2)
+    launches = int(L.lib.viss_launch_count() - n0)
+    acc = batch_accuracy(d, b, cfg)
+    del b, g
+    torch.cuda.empty_cache()
+    # the reference's form: one plain launch pair per channel, on 4 channels
+    pch = [0, nch // 3, 2 * nch // 3, nch - 1]
+    pb = make(pch, cfg.with_(precision=V.PREC_PLAIN))
+    pb.step()
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(st)
+    pb.step()
+    p1.record(st)
+    torch.cuda.synchronize()
+    pterms = 2.0 * pb.K * J
+    plain_value = pterms / (p0.elapsed_time(p1) * 1e-3) / 1e9
+    names = {V.PREC_FAST: "fast", V.PREC_COMPENSATED: "compensated"}
+    line = {"metric": "Gterms/s batched shaded vis-DFT + recon, 1 GB300", "value": round(value, 3), "unit": UNIT,
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fixed-point i32 phase)",
+            "data": "synthetic (seeded orbits per channel + Fibonacci sky)",
+            "config": {"workload": bw.name, "channels": nch, "K": K, "J": J, "terms_per_step": int(terms_step),
+                       "snapshots_per_channel": [int(x) for x in bw.snapshots()], "mask": "geometric",
+                       "precision": names.get(prec, str(prec)), "launch": "CUDA graph: 1 persistent vis + 1 "
+                       "persistent recon kernel (+ prep)", "l2": "flushed (256 MB write) before each timed step"},
+            "vis_ms": round(vis_ms, 2), "recon_ms": round(rec_ms, 2),
+            "autotune": {"best": vars(best), "candidates": report, "timed_on": "channels 0, 8, ..., 56"},
+            "plain_per_channel": {"value": round(plain_value, 3), "unit": UNIT, "channels": pch,
+                                  "what": "PREC_PLAIN, one vis + one recon launch per channel"},
+            "speedup_vs_plain": round(value / plain_value, 2), "accuracy": acc, "clocks": clk.summary(),
+            "gpu_launches_per_step": launches}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def batch_accuracy(d, b, cfg):
+    """FP64 oracle against the batch on a sample of the 30 MHz channel (the largest
+    |uvw|): 32 visibilities x all pixels and 64 pixels x all its visibilities."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    h = lambda t: t.detach().cpu().numpy()  # noqa: E731
+    c = b.nch - 1
+    r0, r1 = int(b.row_off[c]), int(b.row_off[c + 1])
+    u, v, w, snap, pair = (h(d[k][r0:r1]) for k in ("u", "v", "w", "snap", "pair"))
+    pos = h(d["sat_pos"])
+    K = r1 - r0
+    oc = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=cfg.phase_scale, n_offset=cfg.n_offset,
+                    occluded_value=cfg.occluded_value, norm=float(b.norm[c]))
+    rows = np.linspace(0, K - 1, 32).astype(np.int64)
+    Vo = O.vis_dft(oc, u[rows], v[rows], w[rows], d["l"], d["m"], d["n"], h(d["bright"][c]),
+                   geo=O.make_geo(pos, snap[rows], pair[rows]), nthreads=O.max_threads())
+    Vg = h(b.V[r0:r1])
+    pix = np.linspace(0, d["l"].size - 1, 64).astype(np.int64)
+    Fo = O.recon(oc, u, v, w, None, Vg, d["l"][pix], d["m"][pix], d["n"][pix], geo=O.make_geo(pos, snap, pair),
+                 nthreads=O.max_threads())
+    Fg = h(b.F[c])[pix]
+    return {"channel": c, "freq_hz": float(d["freqs"][c]),
+            "vis_rms": float(np.linalg.norm(Vg[rows] - Vo) / np.linalg.norm(Vo)),
+            "recon_rms": float(np.linalg.norm(Fg - Fo) / np.linalg.norm(Fo))}
+
+
 def main():
     args = parse_args()
     ws, rank, local = dist_setup()
+    from viss_recon_shade_gb300.synth import BATCH_WORKLOADS
     if args.impl == "reference":
         run_reference(args, ws, rank, local)
+    elif args.workload in BATCH_WORKLOADS:
+        run_batch(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:

@@ -154,12 +154,89 @@ VISS_API int viss_recon(const viss_dft_cfg* cfg, const viss_sky* sky, const viss
                const viss_geometry* geo, const float* V, float* F, void* workspace,
                size_t workspace_bytes, void* stream);
 
+/* Non-identity fine->coarse sky map (vissGen10M_shade.cu:120-136, 261-286;
+ * vissGen1M_shade_optim1.cu:54-115, 134-171): coarse pixel j's brightness for
+ * visibility k is the mean of its countLoc[j] fine pixels, listed in NXq (in
+ * pixel order, ascending within a pixel), each replaced by the occluded value
+ * inside k's REF window.  NXq as floats (the 10M text files; values are
+ * truncated to integers as the reference does) or as int32 (viss_nxq, the 1M
+ * in-program form): exactly one of NXq_f / NXq_i is set.  Indices outside
+ * [0, X) make the pixel NaN instead of being read. */
+typedef struct viss_fine_map {
+  const float* FF;           /* X fine brightness */
+  const float* NXq_f;
+  const int32_t* NXq_i;
+  const int32_t* countLoc;   /* J */
+  int64_t X;                 /* fine pixels (entries of FF and NXq) */
+} viss_fine_map;
+
+/* Shaded visibility DFT over a fine->coarse map; sky->bright is unused (the
+ * coarse brightness comes from FF).  Same configuration and result layout as
+ * viss_vis_dft. */
+VISS_API size_t viss_vis_dft_map_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_fine_map* map,
+                                           const viss_geometry* geo);
+VISS_API int viss_vis_dft_map(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_fine_map* map,
+                              const viss_vis_set* vis, const viss_geometry* geo, float* V, void* workspace,
+                              size_t workspace_bytes, void* stream);
+
+/* NX -> (countLoc, NXq) (replaces computeLocCount / computeLocViss,
+ * vissGen1M_shade_optim1.cu:54-115): NX holds the 1-based coarse pixel of each
+ * of X fine pixels as floats; countLoc[q] counts the fine pixels with
+ * NX[i] - 1 == q, NXq lists them grouped by q, ascending (the first
+ * sum(countLoc) entries; fine pixels that match no coarse pixel follow). */
+VISS_API size_t viss_nxq_workspace(int64_t X, int64_t J);
+VISS_API int viss_nxq(const float* NX, int64_t X, int64_t J, int32_t* countLoc, int32_t* NXq, void* workspace,
+                      size_t workspace_bytes, void* stream);
+
+/* Batched passes: many frequency channels (or periods) in one persistent
+ * launch.  The reference runs one channel per program run or per OpenMP
+ * iteration (vissGen10M_shade.cu:298-545, one visscal + imagerecon launch pair
+ * per period); here the visibility set holds all channels' rows back to back and
+ * persistent CTAs pull (rows x pixels) work items of every channel from one
+ * queue, so uneven channels (row counts, occluded fractions) share the GPU
+ * without per-channel tails.  The passes enqueue no host synchronisation and
+ * take their scratch from the workspace, so they can be captured in a CUDA graph
+ * once the workspace exists.
+ *   channel c owns visibility rows [row_off[c], row_off[c+1]), row_off[0] = 0,
+ *   row_off[nch] = K; V is K x 2 as for one channel; F is nch x J x 2.
+ * batch = NULL is one channel (exactly viss_vis_dft / viss_recon). */
+#define VISS_MAX_CHANNELS 64
+typedef struct viss_batch {
+  int32_t nch;               /* 1 .. VISS_MAX_CHANNELS */
+  int32_t reserved;
+  const int64_t* row_off;    /* HOST, nch + 1 entries */
+  const float* bright;       /* DEVICE nch x J per-channel brightness (vis); NULL: sky->bright for every channel */
+  const double* norm;        /* HOST nch recon normalisation per channel; NULL: cfg->norm for every channel */
+} viss_batch;
+
+/* Launch choices of the persistent passes (all zero: defaults).  Any values give
+ * the same results up to the order of float additions; viss_recon_shade_gb300's
+ * autotuner times candidates on the caller's own data and picks one. */
+typedef struct viss_tuning {
+  int32_t ctas_per_sm;       /* persistent CTAs per SM (0: as many as fit) */
+  int32_t vis_split;         /* sky chunks per visibility block, each a work item (0: enough for ~4 items per CTA) */
+  int32_t rec_items;         /* recon work items per persistent CTA the row segments aim at (0: 4) */
+  int32_t reserved;
+} viss_tuning;
+
+VISS_API size_t viss_vis_dft_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,
+                                             const viss_geometry* geo, const viss_tuning* tuning);
+VISS_API int viss_vis_dft_batch(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                                const viss_batch* batch, const viss_geometry* geo, const viss_tuning* tuning,
+                                float* V, void* workspace, size_t workspace_bytes, void* stream);
+VISS_API size_t viss_recon_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,
+                                           const viss_geometry* geo, const viss_tuning* tuning);
+VISS_API int viss_recon_batch(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                              const viss_batch* batch, const viss_geometry* geo, const viss_tuning* tuning,
+                              const float* V, float* F, void* workspace, size_t workspace_bytes, void* stream);
+
 /* Reference-shaped operators: the argument lists of the reference kernels
  * (the complex constants I1, CPI, zero, two are implied).  variant selects the
  * brightness arithmetic: VISS_VARIANT_PLAIN truncates FF to int (vissGen10M_shade.cu:128),
  * VISS_VARIANT_OPTIM keeps it float (vissGen10M_shade_optim1.cu:180).
  * NXq/countLoc may both be NULL for the identity fine->coarse map (countLoc = 1,
- * NXq[j] = j); otherwise NXq holds float indices as in the 10M files.
+ * NXq[j] = j); otherwise NXq holds float indices as in the 10M files and FF
+ * the fine brightness (the fine pixel count is taken as sum(countLoc)).
  * mask_mode is VISS_MASK_REF_QUIRK for the reference's behaviour. */
 enum { VISS_VARIANT_PLAIN = 0, VISS_VARIANT_OPTIM = 1 };
 VISS_API int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float* viss,

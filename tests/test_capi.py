@@ -64,3 +64,52 @@ def test_workspace_queries_are_consistent(L):
     assert a > 0 and b > 0 and a % 256 == 0 and b % 256 == 0
     cfg.precision = 0  # plain needs no records
     assert L.lib.viss_vis_dft_workspace(C.byref(cfg), 10000, 5000, C.byref(geo)) < a
+
+
+def _batch(L, row_off, norm=None):
+    import numpy as np
+    ro = np.ascontiguousarray(row_off, dtype=np.int64)
+    nb = None if norm is None else np.ascontiguousarray(norm, dtype=np.float64)
+    b = L.Batch(ro.size - 1, 0, ro.ctypes.data_as(C.POINTER(C.c_int64)), None,
+                None if nb is None else nb.ctypes.data_as(C.POINTER(C.c_double)))
+    b._keep = (ro, nb)
+    return b
+
+
+def test_batch_arguments_checked_on_host(L):
+    cfg = L.DftCfg(0, 0, 1, 0, 0, 0.0, 1.0, -1.0, 1737.4, 1.0)
+    dummy = C.c_void_p(16)
+    sky = L.Sky(dummy, dummy, dummy, dummy, 3)
+    vis = L.VisSet(dummy, dummy, dummy, None, None, None, None, 10)
+    t = L.Tuning(0, 0, 0, 0)
+    for bad in ([1, 10], [0, 4, 3, 10], [0, 4, 9]):  # not from 0, decreasing, not ending at K
+        b = _batch(L, bad)
+        assert L.lib.viss_vis_dft_batch(C.byref(cfg), C.byref(sky), C.byref(vis), C.byref(b), None, C.byref(t),
+                                        dummy, None, 0, None) == L.VISS_ERR_INVALID
+        assert L.lib.viss_recon_batch(C.byref(cfg), C.byref(sky), C.byref(vis), C.byref(b), None, C.byref(t),
+                                      dummy, dummy, None, 0, None) == L.VISS_ERR_INVALID
+        assert L.lib.viss_vis_dft_batch_workspace(C.byref(cfg), C.byref(b), 10, 3, None, None) == 0
+    b = _batch(L, [0] * 66)  # 65 channels
+    assert L.lib.viss_vis_dft_batch(C.byref(cfg), C.byref(sky), C.byref(vis), C.byref(b), None, None, dummy, None, 0,
+                                    None) == L.VISS_ERR_RANGE
+    # trunc_brightness cannot combine with per-channel brightness
+    b = _batch(L, [0, 4, 10])
+    b.bright = dummy
+    cfg.trunc_brightness = 1
+    assert L.lib.viss_vis_dft_batch(C.byref(cfg), C.byref(sky), C.byref(vis), C.byref(b), None, None, dummy, None, 0,
+                                    None) == L.VISS_ERR_UNSUPPORTED
+
+
+def test_batch_workspace_grows_with_channel_padding(L):
+    # every channel is padded to whole blocks of 1024 visibilities in the vis pass
+    cfg = L.DftCfg(3, 2, 1, 0, 0, 0.0, 1.0, -1.0, 1737.4, 1.0)
+    geo = L.Geometry(None, 100, 8, 0)
+    one = L.lib.viss_vis_dft_batch_workspace(C.byref(cfg), None, 10000, 5000, C.byref(geo), None)
+    assert one == L.lib.viss_vis_dft_workspace(C.byref(cfg), 10000, 5000, C.byref(geo))
+    b = _batch(L, [0, 1, 2, 3, 10000])
+    t = L.Tuning(0, 1, 0, 0)  # one sky chunk: no partial sums
+    many = L.lib.viss_vis_dft_batch_workspace(C.byref(cfg), C.byref(b), 10000, 5000, C.byref(geo), C.byref(t))
+    single = L.lib.viss_vis_dft_batch_workspace(C.byref(cfg), None, 10000, 5000, C.byref(geo), C.byref(t))
+    assert many > single
+    r = L.lib.viss_recon_batch_workspace(C.byref(cfg), C.byref(b), 10000, 5000, C.byref(geo), None)
+    assert r > 0 and r % 256 == 0

@@ -131,3 +131,72 @@ def test_mincline_dropin(oracle, tmp_path):
     b = {tuple(r) for r in ref.tolist()}
     assert len(a & b) >= 0.98 * len(b)
     assert np.all(np.diff(ours[:, 0]) >= 0)
+
+
+def make_map_sky_dir(d, res, seed=7):
+    """A res x res fine grid (FF) mapped onto (res/2)^2 coarse pixels (2 x 2 blocks,
+    some fine pixels moved): NX plus, for the 10M layout, countLoc and NXq."""
+    from viss_recon_shade_gb300.synth import fibonacci_sphere
+    rng = np.random.default_rng(seed)
+    X = res * res
+    q, r = np.divmod(np.arange(X), res)
+    coarse = (q // 2) * (res // 2) + (r // 2)
+    J = (res // 2) ** 2
+    moved = rng.choice(X, X // 40, replace=False)
+    coarse[moved] = rng.integers(0, J, moved.size)
+    coarse[coarse == 0] = 1
+    coarse[5] = 0
+    l, m, n = fibonacci_sphere(J)
+    FF = rng.lognormal(3.0, 1.0, X).astype(np.float32)
+    d.mkdir(parents=True, exist_ok=True)
+    write_col(d / "l.txt", l, header=J)
+    write_col(d / "m.txt", m)
+    write_col(d / "n.txt", n)
+    write_col(d / "C.txt", np.zeros(J))
+    write_col(d / "NX.txt", coarse + 1)
+    write_col(d / "FF.txt", FF, header=X)
+    l, m, n = (read_col(d / f).astype(np.float32) for f in ("l.txt", "m.txt", "n.txt"))
+    return l[1:], m, n, read_col(d / "FF.txt").astype(np.float32)[1:], (coarse + 1).astype(np.float32), J
+
+
+def test_vissGen10M_shade_fine_map(oracle, tmp_path):
+    res, K = 64, 1024
+    l, m, n, FF, NX, J = make_map_sky_dir(tmp_path / "lmn10M", res)
+    cl, nq = oracle.nxq(NX, J)
+    write_col(tmp_path / "lmn10M" / "countLoc.txt", cl)
+    write_col(tmp_path / "lmn10M" / "NXq.txt", nq)
+    u, v, w, raw = synth_uvw_shade(K, res, seed=8)
+    fd = tmp_path / "frequency_10M"
+    fd.mkdir()
+    np.savetxt(fd / "updated_uvw1frequency10M.txt", np.stack([u, v, w, np.full(K, 2.0)], -1), fmt="%g")
+    np.savetxt(fd / "shadeM1frequency10M.txt", raw, fmt="%d")
+    run([BIN / "vissGen10M_shade", "--res", res], tmp_path)
+    F = read_col(tmp_path / "F_recon_10M" / "F1period10M.txt")
+    M = oracle.normalise_shade(raw)
+    ncl = np.clip(n, -1, 1)
+    V = oracle.vis_dft_nxq(oracle.make_cfg(mask_mode=1, res=res, trunc=True, occluded_value=240.0), u, v, w, l, m, ncl,
+                           FF, nq.astype(np.float32), cl, shade=M)
+    Fo = oracle.recon(oracle.make_cfg(res=res, recon_ref_mask=True, norm=1.0 / K), u, v, w, np.full(K, 0.5, np.float32),
+                      V.astype(np.complex64), l, m, ncl, shade=M)
+    assert F.shape == (J,)
+    assert np.abs(F - Fo.real).max() / np.abs(Fo.real).max() < 2e-5
+
+
+def test_vissGen1M_fine_map(oracle, tmp_path):
+    res, K = 64, 1024
+    fd = tmp_path / "frequency_1M"
+    l, m, n, FF, NX, J = make_map_sky_dir(fd, res, seed=9)
+    u, v, w, raw = synth_uvw_shade(K, res, seed=10)
+    np.savetxt(fd / "uvw1frequency1M.txt", np.stack([u, v, w], -1), fmt="%g")
+    np.savetxt(fd / "shadeM1frequency1M.txt", raw, fmt="%d")
+    run([BIN / "vissGen1M_shade_optim1", "--res", res], tmp_path)
+    F = read_col(tmp_path / "F_recon_1M" / "F1_optim1.txt")
+    cl, nq = oracle.nxq(NX, J)
+    M = oracle.normalise_shade(raw)
+    V = oracle.vis_dft_nxq(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0), u, v, w, l, m, n, FF,
+                           nq.astype(np.float32), cl, shade=M)
+    Fo = oracle.recon(oracle.make_cfg(res=res, recon_ref_mask=True, norm=1.0 / K), u, v, w, None,
+                      V.astype(np.complex64), l, m, n, shade=M)
+    Ffine = Fo.real[NX.astype(np.int64) - 1]  # expanded to the fine grid
+    assert F.shape == (res * res,)
+    assert np.abs(F - Ffine).max() / np.abs(Ffine).max() < 2e-5

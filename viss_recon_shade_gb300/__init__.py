@@ -5,8 +5,9 @@ shaded direct visibility DFT and the direct-DFT reconstruction, as
 hand-written CUDA kernels behind the C ABI of libvissgb.so
 (include/viss_gb300.h); this package is the Python host side over that ABI.
 """
-from .api import (DftConfig, OrbitConfig, baseline_uvw, dedup_uvw, imagerecon, normalise_shade,  # noqa: F401
-                  orbit_positions, recon, recon_ratios, reference_d, shade_windows, vis_dft, visscal)
+from .api import (ChannelBatch, DftConfig, OrbitConfig, Tuning, autotune, autotune_report,  # noqa: F401
+                  baseline_uvw, dedup_uvw, imagerecon, normalise_shade, nxq, orbit_positions, recon, recon_ratios,
+                  reference_d, shade_windows, tuning_candidates, vis_dft, vis_dft_map, visscal)
 from ._lib import (MASK_GEOMETRIC, MASK_NONE, MASK_REF_INTENDED, MASK_REF_QUIRK, PREC_COMPENSATED,  # noqa: F401
                    PREC_FAST, PREC_PLAIN, RECON_MASK_GEOMETRIC, RECON_MASK_NONE, RECON_MASK_REF, VARIANT_OPTIM,
                    VARIANT_PLAIN, VissError)

@@ -49,6 +49,24 @@ class Geometry(C.Structure):
     _fields_ = [("sat_pos", C.c_void_p), ("S", C.c_int64), ("nsat", C.c_int32), ("reserved", C.c_int32)]
 
 
+class FineMap(C.Structure):
+    _fields_ = [("FF", C.c_void_p), ("NXq_f", C.c_void_p), ("NXq_i", C.c_void_p), ("countLoc", C.c_void_p),
+                ("X", C.c_int64)]
+
+
+MAX_CHANNELS = 64
+
+
+class Batch(C.Structure):
+    _fields_ = [("nch", C.c_int32), ("reserved", C.c_int32), ("row_off", C.POINTER(C.c_int64)),
+                ("bright", C.c_void_p), ("norm", C.POINTER(C.c_double))]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("ctas_per_sm", C.c_int32), ("vis_split", C.c_int32), ("rec_items", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class OrbitCfg(C.Structure):
     _fields_ = [("nsat", C.c_int32), ("orbit_res", C.c_int32), ("orbit_counts", C.c_int32),
                 ("index", C.c_int32), ("a_km", C.c_double), ("e", C.c_double), ("incl_deg", C.c_double),
@@ -70,6 +88,20 @@ _SIGS = {
     "viss_recon_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.c_int64, C.c_int64, C.POINTER(Geometry)]),
     "viss_recon": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Geometry), _P, _P,
                              _P, C.c_size_t, _P]),
+    "viss_vis_dft_batch_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.POINTER(Batch), C.c_int64, C.c_int64,
+                                                  C.POINTER(Geometry), C.POINTER(Tuning)]),
+    "viss_vis_dft_batch": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Batch),
+                                     C.POINTER(Geometry), C.POINTER(Tuning), _P, _P, C.c_size_t, _P]),
+    "viss_recon_batch_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.POINTER(Batch), C.c_int64, C.c_int64,
+                                                C.POINTER(Geometry), C.POINTER(Tuning)]),
+    "viss_recon_batch": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(VisSet), C.POINTER(Batch),
+                                   C.POINTER(Geometry), C.POINTER(Tuning), _P, _P, _P, C.c_size_t, _P]),
+    "viss_vis_dft_map_workspace": (C.c_size_t, [C.POINTER(DftCfg), C.c_int64, C.c_int64, C.POINTER(FineMap),
+                                                C.POINTER(Geometry)]),
+    "viss_vis_dft_map": (C.c_int, [C.POINTER(DftCfg), C.POINTER(Sky), C.POINTER(FineMap), C.POINTER(VisSet),
+                                   C.POINTER(Geometry), _P, _P, C.c_size_t, _P]),
+    "viss_nxq_workspace": (C.c_size_t, [C.c_int64, C.c_int64]),
+    "viss_nxq": (C.c_int, [_P, C.c_int64, C.c_int64, _P, _P, _P, C.c_size_t, _P]),
     "viss_visscal": (C.c_int, [C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,
                                C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, _P]),
     "viss_imagerecon": (C.c_int, [C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,

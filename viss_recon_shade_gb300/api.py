@@ -151,14 +151,225 @@ def recon(cfg: DftConfig, u, v, w, V, l, m, n, wgt=None, shade=None, snap=None, 
     return out
 
 
+# ---------------------------------------------------------------- fine->coarse sky maps
+def nxq(NX: torch.Tensor, J: int):
+    """NX (1-based coarse pixel per fine pixel, float32[X]) -> (countLoc int32[J], NXq int32[X]):
+    the fine pixels of every coarse pixel, ascending (computeLocCount / computeLocViss,
+    vissGen1M_shade_optim1.cu:54-115)."""
+    NX = _dev(NX, torch.float32, "NX")
+    X = NX.numel()
+    countLoc = torch.empty(int(J), dtype=torch.int32, device=NX.device)
+    NXq = torch.empty(X, dtype=torch.int32, device=NX.device)
+    nb = L.lib.viss_nxq_workspace(X, int(J))
+    ws = _workspace(nb, NX.device)
+    L.check(L.lib.viss_nxq(_ptr(NX), X, int(J), _ptr(countLoc), _ptr(NXq), _ptr(ws), nb, _stream()), "viss_nxq")
+    return countLoc, NXq
+
+
+def vis_dft_map(cfg: DftConfig, u, v, w, l, m, n, FF, NXq, countLoc, shade=None, snap=None, pair=None, sat_pos=None,
+                out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """Shaded visibility DFT over a fine->coarse map (visscal with NXq/countLoc,
+    vissGen10M_shade.cu:120-136): coarse pixel j's brightness for row k is the mean of its
+    fine pixels' FF, the occluded value inside k's REF window.  NXq float32 (the 10M files)
+    or int32 (nxq())."""
+    K, J = u.numel(), l.numel()
+    u, v, w = (_dev(x, torch.float32, nm, K) for x, nm in ((u, "u"), (v, "v"), (w, "w")))
+    l, m, n = (_dev(x, torch.float32, nm, J) for x, nm in ((l, "l"), (m, "m"), (n, "n")))
+    FF = _dev(FF, torch.float32, "FF")
+    if NXq.dtype not in (torch.float32, torch.int32):
+        raise TypeError("NXq must be float32 or int32")
+    NXq = _dev(NXq, NXq.dtype, "NXq")
+    countLoc = _dev(countLoc, torch.int32, "countLoc", J)
+    shade = _dev(shade, torch.int32, "shade", K, 4)
+    snap = _dev(snap, torch.int32, "snap", K)
+    pair = _dev(pair, torch.int32, "pair", K)
+    sp, geo = _geometry(sat_pos)
+    X = FF.numel()
+    if NXq.numel() < X:
+        raise ValueError("NXq needs an entry per fine pixel")
+    fm = L.FineMap(FF.data_ptr(), NXq.data_ptr() if NXq.dtype == torch.float32 else None,
+                   NXq.data_ptr() if NXq.dtype == torch.int32 else None, countLoc.data_ptr(), X)
+    if out is None:
+        out = torch.empty(K, dtype=torch.complex64, device=u.device)
+    c = cfg.c(K)
+    ws_bytes = L.lib.viss_vis_dft_map_workspace(C.byref(c), K, J, C.byref(fm), C.byref(geo) if geo else None)
+    ws = _workspace(ws_bytes, u.device)
+    sky = L.Sky(l.data_ptr(), m.data_ptr(), n.data_ptr(), None, J)
+    vs = L.VisSet(u.data_ptr(), v.data_ptr(), w.data_ptr(), None, _ptr(shade), _ptr(snap), _ptr(pair), K)
+    L.check(L.lib.viss_vis_dft_map(C.byref(c), C.byref(sky), C.byref(fm), C.byref(vs), C.byref(geo) if geo else None,
+                                   C.c_void_p(out.data_ptr()), _ptr(ws), ws_bytes, _stream()), "viss_vis_dft_map")
+    return out
+
+
+# ---------------------------------------------------------------- batched channels
+@dataclass(frozen=True)
+class Tuning:
+    """Launch choices of the persistent passes (viss_tuning); zeros are the defaults."""
+    ctas_per_sm: int = 0
+    vis_split: int = 0
+    rec_items: int = 0
+
+    def c(self) -> L.Tuning:
+        return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), 0)
+
+
+class ChannelBatch:
+    """Many frequency channels through one persistent vis launch and one persistent
+    recon launch (viss_vis_dft_batch / viss_recon_batch).
+
+    u, v, w (and snap, pair, wgt, shade) hold every channel's rows back to back;
+    channel c owns rows [row_off[c], row_off[c+1]).  bright is [nch, J]: each
+    channel's sky brightness.  Outputs: V complex64[K] and F complex64[nch, J],
+    allocated once with the workspaces, so that a pass can be captured in a CUDA
+    graph (:meth:`graph`) and replayed.  norm: per-channel recon scale, default
+    1/K_c (the reference's F / amount)."""
+
+    def __init__(self, cfg: DftConfig, u, v, w, row_off, l, m, n, bright, snap=None, pair=None, sat_pos=None,
+                 wgt=None, shade=None, norm=None, tuning: Optional[Tuning] = None):
+        import numpy as np
+        self.K, self.J = u.numel(), l.numel()
+        K, J = self.K, self.J
+        ro = np.ascontiguousarray(np.asarray(row_off, dtype=np.int64))
+        self.nch = ro.size - 1
+        if not (1 <= self.nch <= L.MAX_CHANNELS) or ro[0] != 0 or ro[-1] != K or np.any(np.diff(ro) < 0):
+            raise ValueError("row_off must be 0 = r_0 <= ... <= r_nch = K with 1 <= nch <= 64")
+        self.row_off = ro
+        kc = np.diff(ro)
+        if norm is None:
+            norm = [cfg.norm if cfg.norm is not None else (1.0 / k if k > 0 else 1.0) for k in kc]
+        self.norm = np.ascontiguousarray(np.asarray(norm, dtype=np.float64))
+        if self.norm.size != self.nch:
+            raise ValueError("norm needs one value per channel")
+        self.cfg = cfg
+        self.u, self.v, self.w = (_dev(x, torch.float32, nm, K) for x, nm in ((u, "u"), (v, "v"), (w, "w")))
+        self.l, self.m, self.n = (_dev(x, torch.float32, nm, J) for x, nm in ((l, "l"), (m, "m"), (n, "n")))
+        self.bright = _dev(bright, torch.float32, "bright", self.nch * J)
+        self.wgt = _dev(wgt, torch.float32, "wgt", K)
+        self.shade = _dev(shade, torch.int32, "shade", K, 4)
+        self.snap = _dev(snap, torch.int32, "snap", K)
+        self.pair = _dev(pair, torch.int32, "pair", K)
+        self.sp, self.geo = _geometry(sat_pos)
+        dev = self.u.device
+        self.V = torch.zeros(K, dtype=torch.complex64, device=dev)
+        self.F = torch.zeros(self.nch, J, dtype=torch.complex64, device=dev)
+        self._c = cfg.c(K)
+        self._batch = L.Batch(self.nch, 0, self.row_off.ctypes.data_as(C.POINTER(C.c_int64)), self.bright.data_ptr(),
+                              self.norm.ctypes.data_as(C.POINTER(C.c_double)))
+        self._sky = L.Sky(self.l.data_ptr(), self.m.data_ptr(), self.n.data_ptr(), None, J)
+        self._vs = L.VisSet(self.u.data_ptr(), self.v.data_ptr(), self.w.data_ptr(), _ptr(self.wgt), _ptr(self.shade),
+                            _ptr(self.snap), _ptr(self.pair), K)
+        self.set_tuning(tuning or Tuning())
+
+    def _geo(self):
+        return C.byref(self.geo) if self.geo else None
+
+    def set_tuning(self, tuning: Tuning) -> None:
+        """Choose launch parameters and (re)size the workspaces for them."""
+        self.tuning = tuning
+        self._t = tuning.c()
+        self._vis_ws_bytes = L.lib.viss_vis_dft_batch_workspace(C.byref(self._c), C.byref(self._batch), self.K, self.J,
+                                                                self._geo(), C.byref(self._t))
+        self._rec_ws_bytes = L.lib.viss_recon_batch_workspace(C.byref(self._c), C.byref(self._batch), self.K, self.J,
+                                                              self._geo(), C.byref(self._t))
+        # one buffer serves both passes (they run in order on one stream)
+        self._ws = _workspace(max(self._vis_ws_bytes, self._rec_ws_bytes), self.u.device)
+
+    def vis(self) -> torch.Tensor:
+        """Enqueue the batched vis DFT on the current stream; returns V."""
+        self._sky.bright = None
+        L.check(L.lib.viss_vis_dft_batch(C.byref(self._c), C.byref(self._sky), C.byref(self._vs), C.byref(self._batch),
+                                         self._geo(), C.byref(self._t), C.c_void_p(self.V.data_ptr()), _ptr(self._ws),
+                                         self._vis_ws_bytes, _stream()), "viss_vis_dft_batch")
+        return self.V
+
+    def recon(self, V: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """Enqueue the batched reconstruction of V (default: this batch's V); returns F [nch, J]."""
+        V = self.V if V is None else _dev(V, torch.complex64, "V", self.K)
+        L.check(L.lib.viss_recon_batch(C.byref(self._c), C.byref(self._sky), C.byref(self._vs), C.byref(self._batch),
+                                       self._geo(), C.byref(self._t), C.c_void_p(V.data_ptr()),
+                                       C.c_void_p(self.F.data_ptr()), _ptr(self._ws), self._rec_ws_bytes, _stream()),
+                "viss_recon_batch")
+        return self.F
+
+    def step(self):
+        """vis then recon of every channel."""
+        self.vis()
+        return self.recon()
+
+    def graph(self) -> "torch.cuda.CUDAGraph":
+        """Capture :meth:`step` in a CUDA graph (after one eager warm-up run); replay() re-runs the
+        whole batched pass with one launch call."""
+        s = torch.cuda.Stream(device=self.u.device)
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            self.step()
+        torch.cuda.current_stream().wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.step()
+        return g
+
+
+def tuning_candidates() -> list:
+    """Launch choices the autotuner times: persistent CTAs per SM x recon items per CTA x sky split."""
+    out = []
+    for ctas in (0, 2):
+        for items in (2, 4, 8):
+            out.append(Tuning(ctas_per_sm=ctas, rec_items=items))
+    out.append(Tuning(vis_split=1))
+    out.append(Tuning(vis_split=2))
+    return out
+
+
+_TUNED: dict = {}
+
+
+def autotune(batch: ChannelBatch, candidates=None, reps: int = 1, use_cache: bool = True) -> Tuning:
+    """Time vis + recon of ``batch`` under each candidate Tuning (CUDA events on the current
+    stream, after one warm-up run each) and keep the fastest on the batch.  Results are cached
+    per device and batch shape (channel row counts, J, mask and precision)."""
+    key = (torch.cuda.get_device_name(batch.u.device), tuple(batch.row_off.tolist()), batch.J, batch.cfg.mask,
+           batch.cfg.recon_mask, batch.cfg.precision)
+    if use_cache and key in _TUNED:
+        batch.set_tuning(_TUNED[key][0])
+        return _TUNED[key][0]
+    cands = list(candidates) if candidates is not None else tuning_candidates()
+    times = []
+    for t in cands:
+        batch.set_tuning(t)
+        batch.step()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            batch.step()
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / reps)
+    best = cands[min(range(len(cands)), key=times.__getitem__)]
+    _TUNED[key] = (best, list(zip(cands, times)))
+    batch.set_tuning(best)
+    return best
+
+
+def autotune_report(batch: ChannelBatch):
+    """(tuning, ms) pairs of the last autotune of this batch shape, or None."""
+    key = (torch.cuda.get_device_name(batch.u.device), tuple(batch.row_off.tolist()), batch.J, batch.cfg.mask,
+           batch.cfg.recon_mask, batch.cfg.precision)
+    return _TUNED.get(key, (None, None))[1]
+
+
 # ---------------------------------------------------------------- reference-shaped
 def visscal(uvws_index: int, lmnC_index: int, res: int, FF, viss, u, v, w, l, m, n, shadeM1, shadeM2, shadeM3,
             shadeM4, NXq=None, countLoc=None, dl: float = 2.0, dm: float = 2.0, dn: float = 2.0,
             variant: int = VARIANT_OPTIM, mask: int = MASK_REF_QUIRK, precision: int = PREC_FAST):
     """visscal(...) with the reference's arguments (vissGen10M_shade.cu:108-116); writes viss
-    (complex64[K]) in place.  NXq/countLoc None = identity fine->coarse map."""
+    (complex64[K]) in place.  NXq/countLoc None = identity fine->coarse map; else NXq float32
+    (as the 10M files) and countLoc int32[J], with FF the fine brightness."""
     K, J = int(uvws_index), int(lmnC_index)
-    args = [_dev(x, torch.float32, nm, J) for x, nm in ((FF, "FF"),)]
+    # FF: J coarse values for the identity map, else the fine grid
+    args = [_dev(FF, torch.float32, "FF", J if NXq is None else None)]
+    NXq = _dev(NXq, torch.float32, "NXq")
+    countLoc = _dev(countLoc, torch.int32, "countLoc", J)
     viss = _dev(viss, torch.complex64, "viss", K)
     uu = [_dev(x, torch.float32, nm, K) for x, nm in ((u, "u"), (v, "v"), (w, "w"))]
     pix = [_dev(x, torch.float32, nm, J) for x, nm in ((l, "l"), (m, "m"), (n, "n"))]

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
               "--expt-relaxed-constexpr", f"-I{INCLUDE}", f"-I{CSRC}"] + os.environ.get("VISS_NVCC_FLAGS", "").split()
 
-CU_SOURCES = ["capi.cu", "prep.cu", "vis_dft.cu", "recon.cu", "orbit.cu", "shade.cu", "probe.cu", "order.cu", "noalloc.cu"]
+CU_SOURCES = ["capi.cu", "prep.cu", "vis_dft.cu", "recon.cu", "orbit.cu", "shade.cu", "probe.cu", "order.cu", "noalloc.cu", "finemap.cu"]
 CPP_SOURCES = ["textio.cpp"]
 
 

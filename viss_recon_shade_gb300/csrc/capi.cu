@@ -36,14 +36,73 @@ int launch_prep_recon_ratios(const float* thetaP0, const float* phiP0, const flo
 static inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
 
 // ------------------------------------------------------------------ plans
-// Layout of the workspace of one vis pass.  Chosen from (K, J, mode) only, so
-// the size query and the call agree.
+// Channels of a pass (a single-channel call is a batch of one).
+struct Batch {
+  ChannelRows ch{};
+  const float* bright = nullptr;   // [nch][J] or NULL
+  float norm[VISS_MAX_CH] = {};
+};
+
+// Runtime launch choices (viss_tuning); zeros pick the defaults.
+struct Tuning {
+  int ctas_per_sm = 0;
+  int vis_split = 0;
+  int rec_items = 0;
+};
+
+static int make_batch(const viss_batch* b, int64_t K, const viss_dft_cfg& cfg, Batch& out) {
+  const int nch = b ? b->nch : 1;
+  if (nch < 1 || nch > VISS_MAX_CH) return fail(VISS_ERR_RANGE, "nch must be in [1, 64]");
+  out.ch.nch = nch;
+  out.ch.row_off[0] = 0;
+  for (int c = 0; c < nch; ++c) {
+    const int64_t e = b ? (b->row_off ? b->row_off[c + 1] : -1) : K;
+    if (b && (!b->row_off || b->row_off[0] != 0)) return fail(VISS_ERR_INVALID, "batch row_off must start at 0");
+    if (e < out.ch.row_off[c]) return fail(VISS_ERR_INVALID, "batch row_off must be non-decreasing");
+    out.ch.row_off[c + 1] = e;
+    out.norm[c] = (float)((b && b->norm) ? b->norm[c] : cfg.norm);
+  }
+  if (out.ch.row_off[nch] != K) return fail(VISS_ERR_INVALID, "batch row_off[nch] must equal the visibility count");
+  out.ch.rb_off[0] = 0;
+  for (int c = 0; c < nch; ++c) {
+    const int64_t kc = out.ch.row_off[c + 1] - out.ch.row_off[c];
+    out.ch.rb_off[c + 1] = out.ch.rb_off[c] + (kc + VIS_ROWS - 1) / VIS_ROWS;
+  }
+  out.bright = b ? b->bright : nullptr;
+  return VISS_OK;
+}
+
+static Tuning make_tuning(const viss_tuning* t) {
+  Tuning r;
+  if (t) {
+    r.ctas_per_sm = t->ctas_per_sm > 0 ? t->ctas_per_sm : 0;
+    r.vis_split = t->vis_split > 0 ? t->vis_split : 0;
+    r.rec_items = t->rec_items > 0 ? t->rec_items : 0;
+  }
+  return r;
+}
+
+// Resident CTAs the persistent kernels are planned for.
+static int64_t planned_ctas(const Tuning& t, int minb) {
+  const int per_sm = (t.ctas_per_sm > 0 && t.ctas_per_sm < minb) ? t.ctas_per_sm : minb;
+  return (int64_t)device_sm_count() * per_sm;
+}
+
+// Layout of the workspace of one vis pass.  Chosen from (rows per channel, J,
+// mode, tuning) only, so the size query and the call agree.
 struct VisPlan {
-  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, nrb = 0, jchunk = 0, nsd = 0;
+  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, nrb = 0, jchunk = 0, nsd = 0, X = 0;
   int nsplit = 1;
-  bool geo = false, ref = false, comp = false, plain = false;
-  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *rows1 = nullptr, *win = nullptr;
-  float4 *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *cones = nullptr;
+  bool geo = false, ref = false, comp = false, plain = false, map = false;
+  float* mbase = nullptr;
+  int4* mbox = nullptr;
+  int2 *mmem = nullptr, *mtile = nullptr;
+  int* members = nullptr;
+  char* mscratch = nullptr;
+  size_t mscratch_bytes = 0;
+  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *win = nullptr;
+  float4 *rows1 = nullptr, *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *cones = nullptr;
+  int* rowsat = nullptr;
   int2* pqr = nullptr;
   float2* partial = nullptr;
   int* flags = nullptr;
@@ -51,7 +110,7 @@ struct VisPlan {
 
   void layout(void* ws) {
     Carver c(ws);
-    flags = c.take<int>(64);
+    flags = c.take<int>(FLAG_WORDS);
     if (plain && geo) satdir = c.take<float4>(nsd);
     if (!plain) {
       pix0 = c.take<int4>(Jpad);
@@ -60,31 +119,45 @@ struct VisPlan {
       if (geo) pgeo = c.take<float4>(Jpad);
       if (ref) pqr = c.take<int2>(Jpad);
       rows0 = c.take<int4>(Kpad);
-      rows1 = c.take<int4>(Kpad);
+      rows1 = c.take<float4>(Kpad);
+      if (geo) rowsat = c.take<int>(Kpad);
       if (comp) rowsf = c.take<float4>(Kpad);
       if (ref) win = c.take<int4>(Kpad);
       if (geo) { satdir = c.take<float4>(nsd); cones = c.take<float4>(2 * nrb); }
       if (nsplit > 1) partial = c.take<float2>((size_t)nsplit * K);
+      if (map) {
+        mbase = c.take<float>(Jpad);
+        mbox = c.take<int4>(Jpad);
+        mmem = c.take<int2>(Jpad);
+        mtile = c.take<int2>(Jpad / VIS_P);
+        members = c.take<int>(X > 0 ? X : 1);
+        mscratch_bytes = fine_map_scratch(J);
+        mscratch = c.take<char>(mscratch_bytes);
+      }
     }
     bytes = c.size();
   }
 };
 
-static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, const viss_geometry* geo) {
-  p.K = K; p.J = J;
+static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64_t J, const viss_geometry* geo,
+                     const Tuning& tn, const viss_fine_map* map = nullptr) {
+  p.K = bt.ch.row_off[bt.ch.nch]; p.J = J;
+  p.map = map != nullptr;
+  p.X = map ? map->X : 0;
   p.plain = cfg.precision == VISS_PREC_PLAIN;
   p.geo = cfg.mask_mode == VISS_MASK_GEOMETRIC;
   p.ref = cfg.mask_mode == VISS_MASK_REF_QUIRK || cfg.mask_mode == VISS_MASK_REF_INTENDED;
   p.comp = cfg.precision == VISS_PREC_COMPENSATED;
   p.Jpad = round_up(J > 0 ? J : 1, REC_PIX);
-  p.Kpad = round_up(K > 0 ? K : 1, VIS_ROWS);
-  p.nrb = p.Kpad / VIS_ROWS;
+  p.nrb = bt.ch.rb_off[bt.ch.nch];
+  p.Kpad = (p.nrb > 0 ? p.nrb : 1) * VIS_ROWS;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
-  // Split the pixel axis when the visibility blocks alone fill less than
-  // ~4 waves of resident CTAs.
-  const int64_t slots = (int64_t)device_sm_count() * VISS_VIS_MINB;
+  // Split the pixel axis when the visibility blocks alone give fewer than ~4
+  // work items per resident CTA.
+  const int64_t slots = planned_ctas(tn, VISS_VIS_MINB);
   int64_t nsplit = 1;
-  if (p.nrb < 4 * slots) nsplit = (4 * slots + p.nrb - 1) / p.nrb;
+  if (tn.vis_split > 0) nsplit = tn.vis_split;
+  else if (p.nrb > 0 && p.nrb < 4 * slots) nsplit = (4 * slots + p.nrb - 1) / p.nrb;
   const int64_t maxsplit = (J + VIS_P - 1) / VIS_P;
   if (nsplit > maxsplit) nsplit = maxsplit;
   if (nsplit < 1) nsplit = 1;
@@ -96,13 +169,17 @@ static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, 
 }
 
 struct RecPlan {
-  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, npb = 0, kchunk = 0, nsd = 0, S = 0;
-  int nsplit = 1;
+  int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, npb = 0, nsd = 0, S = 0;
+  int nseg = 0, nslot = 0;
+  int64_t seg_lo[VISS_MAX_SEG] = {}, seg_hi[VISS_MAX_SEG] = {};
+  int seg_ch[VISS_MAX_SEG] = {}, seg_slot[VISS_MAX_SEG] = {};
+  int slot0[VISS_MAX_CH] = {}, nslot_ch[VISS_MAX_CH] = {};
   bool geo = false, ref = false, comp = false, plain = false;
-  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *rows1 = nullptr, *win = nullptr;
-  float4 *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *scones = nullptr;
+  int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *win = nullptr;
+  float4 *rows1 = nullptr, *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *scones = nullptr;
+  int* rowsat = nullptr;
   int2* pqr = nullptr;
-  float2 *y = nullptr, *partial = nullptr;
+  float2* partial = nullptr;
   float* ratios = nullptr;
   int* flags = nullptr;
   int32_t* perm = nullptr;
@@ -112,7 +189,7 @@ struct RecPlan {
 
   void layout(void* ws) {
     Carver c(ws);
-    flags = c.take<int>(64);
+    flags = c.take<int>(FLAG_WORDS);
     if (plain) {
       if (ref) ratios = c.take<float>(2 * (size_t)Kpad);
       if (geo) satdir = c.take<float4>(nsd);
@@ -128,38 +205,76 @@ struct RecPlan {
       if (geo) pgeo = c.take<float4>(Jpad);
       if (ref) pqr = c.take<int2>(Jpad);
       rows0 = c.take<int4>(Kpad);
-      rows1 = c.take<int4>(Kpad);
+      rows1 = c.take<float4>(Kpad);
+      if (geo) rowsat = c.take<int>(Kpad);
       if (comp) rowsf = c.take<float4>(Kpad);
       if (ref) win = c.take<int4>(Kpad);
-      y = c.take<float2>(Kpad);
       if (geo) { satdir = c.take<float4>(nsd); scones = c.take<float4>(2 * S); }
-      if (nsplit > 1) partial = c.take<float2>((size_t)nsplit * J);
+      if (nslot > 0) partial = c.take<float2>((size_t)nslot * J);
     }
     bytes = c.size();
   }
 };
 
-static void plan_recon(RecPlan& p, const viss_dft_cfg& cfg, int64_t K, int64_t J, const viss_geometry* geo) {
-  p.K = K; p.J = J;
+// Recon work: every channel's rows cut into segments of about L rows, L chosen
+// for ~rec_items work items (segment x pixel block) per resident CTA; at most
+// VISS_MAX_SEG segments.  Segments are ordered longest first.
+static void plan_segments(RecPlan& p, const Batch& bt, const Tuning& tn) {
+  constexpr int64_t unit = REC_Q;
+  const int nch = bt.ch.nch;
+  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 4) * planned_ctas(tn, VISS_REC_MINB);
+  int64_t L = p.npb > 0 ? (p.K * p.npb + target - 1) / target : p.K;
+  L = round_up(L > unit ? L : unit, unit);
+  auto count = [&](int64_t len) {
+    int64_t n = 0;
+    for (int c = 0; c < nch; ++c) {
+      const int64_t kc = bt.ch.row_off[c + 1] - bt.ch.row_off[c];
+      n += (kc + len - 1) / len;
+    }
+    return n;
+  };
+  while (count(L) > VISS_MAX_SEG) L = round_up(L + L / 4 + 1, unit);
+  struct Seg { int64_t lo, hi; int ch, idx; };
+  Seg segs[VISS_MAX_SEG];
+  int ns = 0, slots = 0;
+  for (int c = 0; c < nch; ++c) {
+    const int64_t r0 = bt.ch.row_off[c], kc = bt.ch.row_off[c + 1] - r0;
+    const int64_t n = (kc + L - 1) / L;
+    p.slot0[c] = slots;
+    p.nslot_ch[c] = n > 1 ? (int)n : 0;
+    for (int64_t i = 0; i < n; ++i) {
+      segs[ns] = Seg{r0 + kc * i / n, r0 + kc * (i + 1) / n, c, n > 1 ? slots + (int)i : -1};
+      ++ns;
+    }
+    if (n > 1) slots += (int)n;
+  }
+  // longest first (stable)
+  for (int i = 1; i < ns; ++i) {
+    const Seg s = segs[i];
+    int j = i - 1;
+    while (j >= 0 && segs[j].hi - segs[j].lo < s.hi - s.lo) { segs[j + 1] = segs[j]; --j; }
+    segs[j + 1] = s;
+  }
+  p.nseg = ns;
+  p.nslot = slots;
+  for (int i = 0; i < ns; ++i) {
+    p.seg_lo[i] = segs[i].lo; p.seg_hi[i] = segs[i].hi; p.seg_ch[i] = segs[i].ch; p.seg_slot[i] = segs[i].idx;
+  }
+}
+
+static void plan_recon(RecPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64_t J, const viss_geometry* geo,
+                       const Tuning& tn) {
+  p.K = bt.ch.row_off[bt.ch.nch]; p.J = J;
   p.plain = cfg.precision == VISS_PREC_PLAIN;
   p.geo = cfg.recon_mask == VISS_RECON_MASK_GEOMETRIC;
   p.ref = cfg.recon_mask == VISS_RECON_MASK_REF;
   p.comp = cfg.precision == VISS_PREC_COMPENSATED;
   p.Jpad = round_up(J > 0 ? J : 1, REC_PIX);
-  p.Kpad = round_up(K > 0 ? K : 1, VIS_ROWS);
+  p.Kpad = p.K > 0 ? p.K : 1;
   p.npb = p.Jpad / REC_PIX;
   p.S = (geo && p.geo) ? geo->S : 0;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
-  const int64_t slots = (int64_t)device_sm_count() * VISS_REC_MINB;
-  int64_t nsplit = 1;
-  if (p.npb < 4 * slots) nsplit = (4 * slots + p.npb - 1) / p.npb;
-  const int64_t maxsplit = (K + REC_Q - 1) / REC_Q;
-  if (nsplit > maxsplit) nsplit = maxsplit;
-  if (nsplit < 1) nsplit = 1;
-  p.kchunk = round_up((K + nsplit - 1) / nsplit, REC_Q);
-  if (p.kchunk <= 0) p.kchunk = REC_Q;
-  p.nsplit = (int)((K + p.kchunk - 1) / p.kchunk);
-  if (p.nsplit < 1) p.nsplit = 1;
+  if (!p.plain) plan_segments(p, bt, tn);
   p.layout(nullptr);
 }
 
@@ -213,11 +328,22 @@ static int check_ws(void* ws, size_t have, size_t need) {
 }
 
 // ------------------------------------------------------------------ passes
+static viss_vis_set channel_rows(const viss_vis_set& vis, int64_t r0, int64_t r1) {
+  viss_vis_set c = vis;
+  c.u = vis.u + r0; c.v = vis.v + r0; c.w = vis.w + r0;
+  if (vis.wgt) c.wgt = vis.wgt + r0;
+  if (vis.shade) c.shade = vis.shade + 4 * r0;
+  if (vis.snap) c.snap = vis.snap + r0;
+  if (vis.pair) c.pair = vis.pair + r0;
+  c.K = r1 - r0;
+  return c;
+}
+
 int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
-                 const viss_vis_set& vis, const viss_geometry* geo, float* V, void* ws, size_t ws_bytes,
-                 cudaStream_t st) {
+                 const viss_vis_set& vis, const Batch& bt, const viss_geometry* geo, const Tuning& tn, float* V,
+                 void* ws, size_t ws_bytes, cudaStream_t st, const viss_fine_map* map = nullptr) {
   VisPlan p;
-  plan_vis(p, cfg, vis.K, sky.J, geo);
+  plan_vis(p, cfg, bt, sky.J, geo, tn, map);
   int rc = check_ws(ws, ws_bytes, p.bytes);
   if (rc) return rc;
   if (vis.K == 0) return VISS_OK;
@@ -227,15 +353,29 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   }
   p.layout(ws);
   if (p.plain) {
+    // the reference's form: one launch per channel
     if (p.geo && (rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
-    return launch_vis_plain(cfg, sky, vis, geo, p.satdir, dlmn, reinterpret_cast<float2*>(V), st);
+    for (int c = 0; c < bt.ch.nch; ++c) {
+      const int64_t r0 = bt.ch.row_off[c], r1 = bt.ch.row_off[c + 1];
+      if (r1 == r0) continue;
+      viss_sky sc = sky;
+      if (bt.bright) sc.bright = bt.bright + (int64_t)c * sky.J;
+      if ((rc = launch_vis_plain(cfg, sc, channel_rows(vis, r0, r1), geo, p.satdir, dlmn,
+                                 reinterpret_cast<float2*>(V) + r0, st, map)))
+        return rc;
+    }
+    return VISS_OK;
   }
-  VISS_CUDA(cudaMemsetAsync(p.flags, 0, 64 * sizeof(int), st));
+  VISS_CUDA(cudaMemsetAsync(p.flags, 0, FLAG_WORDS * sizeof(int), st));
+  if (map && (rc = prep_fine_map(map->NXq_f, map->NXq_i, map->countLoc, map->FF, sky.J, map->X, cfg.res,
+                                 cfg.trunc_brightness, p.Jpad, p.mbase, p.mbox, p.mmem, p.members, p.mtile,
+                                 p.mscratch, p.mscratch_bytes, p.flags, st)))
+    return rc;
   PixPrepArgs pa{};
-  pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = sky.bright;
+  pa.l = sky.l; pa.m = sky.m; pa.n = sky.n; pa.bright = bt.bright ? nullptr : (map ? p.mbase : sky.bright);
   pa.J = sky.J; pa.Jpad = p.Jpad;
   pa.sl = scale[0]; pa.sm = scale[1]; pa.sn = scale[2]; pa.n_offset = cfg.n_offset;
-  pa.res = cfg.res; pa.trunc = cfg.trunc_brightness;
+  pa.res = cfg.res; pa.trunc = map ? 0 : cfg.trunc_brightness;  // the map's base brightness is truncated per member
   pa.rec0 = p.pix0; pa.rec1 = p.pix1; pa.lo = p.plo; pa.geo = p.pgeo; pa.qr = p.pqr;
   if ((rc = launch_prep_pixels(pa, st))) return rc;
   RowPrepArgs ra{};
@@ -243,58 +383,85 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
   ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
   ra.sn = scale[2]; ra.n_offset = cfg.n_offset;
+  ra.ch = bt.ch; ra.padded = true;
   ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = cfg.mask_mode; ra.recon_mask = VISS_RECON_MASK_NONE;
-  ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.flags = p.flags;
+  ra.rows0 = p.rows0; ra.rows1 = p.rows1; ra.rowsat = p.rowsat; ra.uf = p.rowsf; ra.win = p.win;
+  ra.flags = p.flags;
   if ((rc = launch_prep_rows(ra, false, st))) return rc;
   if (p.geo) {
     if ((rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
-    if ((rc = launch_prep_rowblock_cones(p.rows0, p.rows1, p.satdir, vis.K, VIS_ROWS, p.nrb, p.cones, st)))
-      return rc;
+    if ((rc = launch_prep_rowblock_cones(p.rowsat, p.satdir, bt.ch, p.nrb, p.cones, st))) return rc;
   }
   VisParams vp{};
   vp.pix0 = p.pix0; vp.pix1 = p.pix1; vp.plo = p.plo; vp.pgeo = p.pgeo; vp.pqr = p.pqr;
-  vp.rows0 = p.rows0; vp.rows1 = p.rows1; vp.rowsf = p.rowsf; vp.win = p.win;
+  vp.rows0 = p.rows0; vp.rows1 = p.rows1; vp.rowsat = p.rowsat; vp.rowsf = p.rowsf; vp.win = p.win;
   vp.satdir = p.satdir; vp.cones = p.cones;
   vp.l = sky.l; vp.m = sky.m; vp.n = sky.n; vp.sat_pos = geo ? geo->sat_pos : nullptr;
+  vp.bright = bt.bright;
   vp.flags = p.flags;
   vp.out = p.nsplit > 1 ? p.partial : reinterpret_cast<float2*>(V);
   vp.K = vis.K; vp.J = sky.J; vp.jchunk = p.jchunk; vp.nsplit = p.nsplit;
+  vp.nitems = (int)(p.nrb * p.nsplit);
   vp.res = cfg.res > 0 ? cfg.res : 1; vp.occ_val = cfg.occluded_value; vp.R = cfg.moon_radius_km;
   vp.mask = cfg.mask_mode;
-  if ((rc = launch_vis_fast(vp, p.nrb, p.comp, st))) return rc;
+  vp.ch = bt.ch;
+  if (map) {
+    vp.use_map = 1;
+    vp.map.box = p.mbox; vp.map.mem = p.mmem; vp.map.members = p.members; vp.map.FF = map->FF;
+    vp.map.tile_rng = p.mtile; vp.map.trunc = cfg.trunc_brightness;
+  }
+  if ((rc = launch_vis_fast(vp, tn.ctas_per_sm, p.comp, st))) return rc;
   if (p.nsplit > 1) return launch_vis_reduce(p.partial, p.nsplit, vis.K, reinterpret_cast<float2*>(V), st);
   return VISS_OK;
 }
 
 int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
-               const viss_vis_set& vis, const viss_geometry* geo, const float* V, float* F, void* ws,
-               size_t ws_bytes, cudaStream_t st, const float* ratio_arrays[4]) {
+               const viss_vis_set& vis, const Batch& bt, const viss_geometry* geo, const Tuning& tn, const float* V,
+               float* F, void* ws, size_t ws_bytes, cudaStream_t st, const float* ratio_arrays[4]) {
   RecPlan p;
-  plan_recon(p, cfg, vis.K, sky.J, geo);
+  plan_recon(p, cfg, bt, sky.J, geo, tn);
   int rc = check_ws(ws, ws_bytes, p.bytes);
   if (rc) return rc;
   if (sky.J == 0) return VISS_OK;
   if (vis.K == 0) {
-    VISS_CUDA(cudaMemsetAsync(F, 0, sizeof(float2) * (size_t)sky.J, st));
+    VISS_CUDA(cudaMemsetAsync(F, 0, sizeof(float2) * (size_t)sky.J * bt.ch.nch, st));
     return VISS_OK;
   }
   p.layout(ws);
-  VISS_CUDA(cudaMemsetAsync(p.flags, 0, 64 * sizeof(int), st));
+  VISS_CUDA(cudaMemsetAsync(p.flags, 0, FLAG_WORDS * sizeof(int), st));
+  float2* const F2 = reinterpret_cast<float2*>(F);
+  // channels without visibilities reconstruct to zero
+  for (int c = 0; c < bt.ch.nch; ++c)
+    if (bt.ch.row_off[c + 1] == bt.ch.row_off[c])
+      VISS_CUDA(cudaMemsetAsync(F2 + (int64_t)c * sky.J, 0, sizeof(float2) * (size_t)sky.J, st));
   if (p.plain) {
-    const float* ratios = nullptr;
-    if (p.ref) {
-      if (ratio_arrays) {
-        VISS_CUDA(cudaMemcpyAsync(p.ratios, ratio_arrays[0], sizeof(float) * vis.K, cudaMemcpyDeviceToDevice, st));
-        VISS_CUDA(cudaMemcpyAsync(p.ratios + vis.K, ratio_arrays[1], sizeof(float) * vis.K,
-                                  cudaMemcpyDeviceToDevice, st));
-      } else {
-        extern int launch_shade_ratios(const int32_t* shade, int64_t K, float* r, cudaStream_t st);
-        if ((rc = launch_shade_ratios(vis.shade, vis.K, p.ratios, st))) return rc;
-      }
-      ratios = p.ratios;
-    }
+    // the reference's form: one launch per channel
     if (p.geo && (rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
-    return launch_recon_plain(cfg, sky, vis, geo, V, ratios, p.satdir, dlmn, reinterpret_cast<float2*>(F), st);
+    for (int c = 0; c < bt.ch.nch; ++c) {
+      const int64_t r0 = bt.ch.row_off[c], r1 = bt.ch.row_off[c + 1];
+      if (r1 == r0) continue;
+      const viss_vis_set vc = channel_rows(vis, r0, r1);
+      const float* ratios = nullptr;
+      if (p.ref) {
+        float* rc_ratios = p.ratios + 2 * r0;  // [r1 (K_c), r2 (K_c)]
+        if (ratio_arrays) {
+          VISS_CUDA(cudaMemcpyAsync(rc_ratios, ratio_arrays[0] + r0, sizeof(float) * vc.K, cudaMemcpyDeviceToDevice,
+                                    st));
+          VISS_CUDA(cudaMemcpyAsync(rc_ratios + vc.K, ratio_arrays[1] + r0, sizeof(float) * vc.K,
+                                    cudaMemcpyDeviceToDevice, st));
+        } else {
+          extern int launch_shade_ratios(const int32_t* shade, int64_t K, float* r, cudaStream_t st);
+          if ((rc = launch_shade_ratios(vc.shade, vc.K, rc_ratios, st))) return rc;
+        }
+        ratios = rc_ratios;
+      }
+      viss_dft_cfg cc = cfg;
+      cc.norm = bt.norm[c];
+      if ((rc = launch_recon_plain(cc, sky, vc, geo, V + 2 * r0, ratios, p.satdir, dlmn, F2 + (int64_t)c * sky.J,
+                                   st)))
+        return rc;
+    }
+    return VISS_OK;
   }
   if (p.geo) {
     if ((rc = pixel_order(sky.l, sky.m, sky.n, sky.J, p.order_scratch, p.order_bytes, p.perm, st))) return rc;
@@ -313,8 +480,10 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
   ra.nsat = geo ? geo->nsat : 0; ra.S = geo ? geo->S : 0;
   ra.sn = scale[2]; ra.n_offset = cfg.n_offset;
+  ra.ch = bt.ch; ra.padded = false;
   ra.K = vis.K; ra.Kpad = p.Kpad; ra.mask_mode = VISS_MASK_NONE; ra.recon_mask = cfg.recon_mask;
-  ra.rec0 = p.rows0; ra.rec1 = p.rows1; ra.uf = p.rowsf; ra.win = p.win; ra.y = p.y; ra.flags = p.flags;
+  ra.rows0 = p.rows0; ra.rows1 = p.rows1; ra.rowsat = p.rowsat; ra.uf = p.rowsf; ra.win = p.win;
+  ra.flags = p.flags;
   if ((rc = launch_prep_rows(ra, true, st))) return rc;
   if (p.ref && ratio_arrays) {
     if ((rc = launch_prep_recon_ratios(ratio_arrays[0], ratio_arrays[1], ratio_arrays[2], ratio_arrays[3], vis.K,
@@ -327,18 +496,57 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   }
   ReconParams rp{};
   rp.pix0 = p.pix0; rp.pix1 = p.pix1; rp.plo = p.plo; rp.pgeo = p.pgeo; rp.pqr = p.pqr;
-  rp.rows0 = p.rows0; rp.rows1 = p.rows1; rp.rowsf = p.rowsf; rp.win = p.win; rp.y = p.y;
+  rp.rows0 = p.rows0; rp.rows1 = p.rows1; rp.rowsat = p.rowsat; rp.rowsf = p.rowsf; rp.win = p.win;
   rp.satdir = p.satdir; rp.scones = p.scones;
   rp.l = sky.l; rp.m = sky.m; rp.n = sky.n; rp.sat_pos = geo ? geo->sat_pos : nullptr;
   rp.flags = p.flags;
   rp.perm = p.perm;
-  rp.out = p.nsplit > 1 ? p.partial : reinterpret_cast<float2*>(F);
-  rp.K = vis.K; rp.J = sky.J; rp.kchunk = p.kchunk; rp.nsplit = p.nsplit;
+  rp.out = F2;
+  rp.partial = p.partial;
+  rp.K = vis.K; rp.J = sky.J;
   rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
-  rp.norm = (float)cfg.norm; rp.recon_mask = cfg.recon_mask;
-  if ((rc = launch_recon_fast(rp, p.npb, p.comp, st))) return rc;
-  if (p.nsplit > 1)
-    return launch_recon_reduce(p.partial, p.nsplit, sky.J, (float)cfg.norm, p.perm, reinterpret_cast<float2*>(F), st);
+  rp.recon_mask = cfg.recon_mask;
+  rp.npb = (int)p.npb;
+  rp.nseg = p.nseg;
+  rp.nitems = (int)(p.nseg * p.npb);
+  for (int i = 0; i < p.nseg; ++i) {
+    rp.seg_lo[i] = p.seg_lo[i]; rp.seg_hi[i] = p.seg_hi[i]; rp.seg_ch[i] = p.seg_ch[i]; rp.seg_slot[i] = p.seg_slot[i];
+  }
+  for (int c = 0; c < bt.ch.nch; ++c) rp.ch_norm[c] = bt.norm[c];
+  if ((rc = launch_recon_fast(rp, tn.ctas_per_sm, p.comp, st))) return rc;
+  if (p.nslot > 0) {
+    RecReduceParams rr{};
+    rr.partial = p.partial; rr.perm = p.perm; rr.out = F2; rr.J = sky.J; rr.nch = bt.ch.nch;
+    for (int c = 0; c < bt.ch.nch; ++c) { rr.slot0[c] = p.slot0[c]; rr.nslot[c] = p.nslot_ch[c]; rr.norm[c] = bt.norm[c]; }
+    return launch_recon_reduce(rr, st);
+  }
+  return VISS_OK;
+}
+
+__global__ void sum_counts_kernel(const int32_t* c, int64_t n, unsigned long long* out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  long long v = i < n ? (long long)c[i] : 0;
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v != 0) atomicAdd(out, (unsigned long long)v);
+}
+
+// sum of n device ints, read back to the host (synchronises the stream)
+int sum_counts(const int32_t* c, int64_t n, int64_t* total, cudaStream_t st) {
+  unsigned long long* d = nullptr;
+  VISS_CUDA(cudaMallocAsync(&d, sizeof(unsigned long long), st));
+  unsigned long long h = 0;
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(h), st);
+  if (e == cudaSuccess && n > 0) {
+    sum_counts_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(c, n, d);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) count_launch();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+  cudaError_t e2 = cudaFreeAsync(d, st);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "sum of countLoc");
+  *total = (int64_t)(long long)h;
   return VISS_OK;
 }
 
@@ -391,39 +599,117 @@ int viss_version(void) { return 10000; }
 uint64_t viss_launch_count(void) { return g_launches; }
 
 size_t viss_vis_dft_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo) {
-  if (!cfg) return 0;
+  return viss_vis_dft_batch_workspace(cfg, nullptr, K, J, geo, nullptr);
+}
+
+size_t viss_vis_dft_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,
+                                    const viss_geometry* geo, const viss_tuning* tuning) {
+  if (!cfg || K < 0 || J < 0) return 0;
+  Batch bt;
+  if (make_batch(batch, K, *cfg, bt)) return 0;
   VisPlan p;
-  plan_vis(p, *cfg, K, J, geo);
+  plan_vis(p, *cfg, bt, J, geo, make_tuning(tuning));
   return p.bytes;
+}
+
+static int check_vis_call(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                          const viss_geometry* geo, const viss_batch* batch, const float* V) {
+  int rc;
+  const bool own_bright = batch && batch->bright;
+  if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, !own_bright)) || (rc = check_vis(vis))) return rc;
+  if (vis->K > 0 && !V) return fail(VISS_ERR_INVALID, "V is NULL");
+  if ((cfg->mask_mode == VISS_MASK_REF_QUIRK || cfg->mask_mode == VISS_MASK_REF_INTENDED)) {
+    if (!vis->shade) return fail(VISS_ERR_INVALID, "REF mask needs shade windows");
+    if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF mask needs res >= 1");
+  }
+  if (own_bright && cfg->trunc_brightness && cfg->precision != VISS_PREC_PLAIN)
+    return fail(VISS_ERR_UNSUPPORTED, "trunc_brightness with per-channel brightness");
+  if (cfg->mask_mode == VISS_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  return VISS_OK;
 }
 
 int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis, const viss_geometry* geo,
                  float* V, void* workspace, size_t workspace_bytes, void* stream) {
+  return viss_vis_dft_batch(cfg, sky, vis, nullptr, geo, nullptr, V, workspace, workspace_bytes, stream);
+}
+
+int viss_vis_dft_batch(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
+                       const viss_batch* batch, const viss_geometry* geo, const viss_tuning* tuning, float* V,
+                       void* workspace, size_t workspace_bytes, void* stream) {
   int rc;
-  if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, true)) || (rc = check_vis(vis))) return rc;
+  if ((rc = check_vis_call(cfg, sky, vis, geo, batch, V))) return rc;
+  Batch bt;
+  if ((rc = make_batch(batch, vis->K, *cfg, bt))) return rc;
+  const double s = cfg->phase_scale;
+  const double scale[3] = {s, s, s};
+  const float d = (float)(1.0 / s);
+  const float dlmn[3] = {d, d, d};
+  return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, bt, geo, make_tuning(tuning), V, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream));
+}
+
+static int check_map(const viss_fine_map* map, int64_t J) {
+  if (!map) return fail(VISS_ERR_INVALID, "fine map is NULL");
+  if (map->X < 0 || map->X > ((int64_t)1 << 31) - 1) return fail(VISS_ERR_RANGE, "fine map X out of range");
+  if (J > 0 && !map->countLoc) return fail(VISS_ERR_INVALID, "fine map countLoc is NULL");
+  if (map->X > 0 && (!map->FF || (!map->NXq_f == !map->NXq_i)))
+    return fail(VISS_ERR_INVALID, "fine map needs FF and exactly one of NXq_f / NXq_i");
+  return VISS_OK;
+}
+
+size_t viss_vis_dft_map_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_fine_map* map,
+                                  const viss_geometry* geo) {
+  if (!cfg || !map || K < 0 || J < 0) return 0;
+  Batch bt;
+  if (make_batch(nullptr, K, *cfg, bt)) return 0;
+  VisPlan p;
+  plan_vis(p, *cfg, bt, J, geo, Tuning{}, map);
+  return p.bytes;
+}
+
+int viss_vis_dft_map(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_fine_map* map, const viss_vis_set* vis,
+                     const viss_geometry* geo, float* V, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc;
+  if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, false)) || (rc = check_vis(vis))) return rc;
+  if ((rc = check_map(map, sky->J))) return rc;
   if (vis->K > 0 && !V) return fail(VISS_ERR_INVALID, "V is NULL");
   if ((cfg->mask_mode == VISS_MASK_REF_QUIRK || cfg->mask_mode == VISS_MASK_REF_INTENDED)) {
     if (!vis->shade) return fail(VISS_ERR_INVALID, "REF mask needs shade windows");
     if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF mask needs res >= 1");
   }
   if (cfg->mask_mode == VISS_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  Batch bt;
+  if ((rc = make_batch(nullptr, vis->K, *cfg, bt))) return rc;
   const double s = cfg->phase_scale;
   const double scale[3] = {s, s, s};
   const float d = (float)(1.0 / s);
   const float dlmn[3] = {d, d, d};
-  return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, geo, V, workspace, workspace_bytes,
-                      static_cast<cudaStream_t>(stream));
+  return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, bt, geo, Tuning{}, V, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream), map);
 }
 
 size_t viss_recon_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_geometry* geo) {
-  if (!cfg) return 0;
+  return viss_recon_batch_workspace(cfg, nullptr, K, J, geo, nullptr);
+}
+
+size_t viss_recon_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,
+                                  const viss_geometry* geo, const viss_tuning* tuning) {
+  if (!cfg || K < 0 || J < 0) return 0;
+  Batch bt;
+  if (make_batch(batch, K, *cfg, bt)) return 0;
   RecPlan p;
-  plan_recon(p, *cfg, K, J, geo);
+  plan_recon(p, *cfg, bt, J, geo, make_tuning(tuning));
   return p.bytes;
 }
 
 int viss_recon(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis, const viss_geometry* geo,
                const float* V, float* F, void* workspace, size_t workspace_bytes, void* stream) {
+  return viss_recon_batch(cfg, sky, vis, nullptr, geo, nullptr, V, F, workspace, workspace_bytes, stream);
+}
+
+int viss_recon_batch(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis, const viss_batch* batch,
+                     const viss_geometry* geo, const viss_tuning* tuning, const float* V, float* F,
+                     void* workspace, size_t workspace_bytes, void* stream) {
   int rc;
   if ((rc = check_cfg(cfg)) || (rc = check_sky(sky, false)) || (rc = check_vis(vis))) return rc;
   if (sky->J > 0 && !F) return fail(VISS_ERR_INVALID, "F is NULL");
@@ -433,11 +719,13 @@ int viss_recon(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set*
     if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF recon mask needs res >= 1");
   }
   if (cfg->recon_mask == VISS_RECON_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  Batch bt;
+  if ((rc = make_batch(batch, vis->K, *cfg, bt))) return rc;
   const double s = cfg->phase_scale;
   const double scale[3] = {s, s, s};
   const float d = (float)(1.0 / s);
   const float dlmn[3] = {d, d, d};
-  return recon_impl(*cfg, scale, dlmn, *sky, *vis, geo, V, F, workspace, workspace_bytes,
+  return recon_impl(*cfg, scale, dlmn, *sky, *vis, bt, geo, make_tuning(tuning), V, F, workspace, workspace_bytes,
                     static_cast<cudaStream_t>(stream), nullptr);
 }
 
@@ -446,8 +734,7 @@ int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float
                  const int* shadeM2, const int* shadeM3, const int* shadeM4, const float* NXq, const int* countLoc,
                  float dl, float dm, float dn, int variant, int mask_mode, int precision, void* stream) {
   if (uvws_index < 0 || lmnC_index < 0) return fail(VISS_ERR_RANGE, "negative size");
-  if (NXq || countLoc)
-    return fail(VISS_ERR_UNSUPPORTED, "non-identity fine->coarse map (NXq/countLoc) is not supported here");
+  if (!NXq != !countLoc) return fail(VISS_ERR_INVALID, "NXq and countLoc go together (both NULL: identity map)");
   if (!(dl > 0.f && dm > 0.f && dn > 0.f)) return fail(VISS_ERR_RANGE, "dl, dm, dn must be > 0");
   if (mask_mode != VISS_MASK_NONE && mask_mode != VISS_MASK_REF_QUIRK && mask_mode != VISS_MASK_REF_INTENDED)
     return fail(VISS_ERR_INVALID, "viss_visscal takes NONE or a REF mask");
@@ -471,8 +758,16 @@ int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float
   viss_vis_set vis{u, v, w, nullptr, nullptr, nullptr, nullptr, uvws_index};
   const double scale[3] = {1.0 / dl, 1.0 / dm, 1.0 / dn};
   const float dlmn[3] = {dl, dm, dn};
+  viss_fine_map map{FF, NXq, nullptr, countLoc, 0};
+  if (countLoc) {
+    // the fine pixel count is not among the reference's arguments: sum(countLoc)
+    if ((rc = sum_counts(countLoc, lmnC_index, &map.X, st))) return rc;
+    sky.bright = nullptr;
+  }
+  Batch bt;
+  if ((rc = make_batch(nullptr, uvws_index, cfg, bt))) return rc;
   VisPlan p;
-  plan_vis(p, cfg, uvws_index, lmnC_index, nullptr);
+  plan_vis(p, cfg, bt, lmnC_index, nullptr, Tuning{}, countLoc ? &map : nullptr);
   const size_t shade_bytes = mask_mode != VISS_MASK_NONE ? ((sizeof(int4) * (size_t)uvws_index + 255) & ~size_t(255)) : 0;
   void* ws = nullptr;
   const size_t total = p.bytes + shade_bytes;
@@ -484,7 +779,8 @@ int viss_visscal(int uvws_index, int lmnC_index, int res, const float* FF, float
     VISS_LAUNCH_CHECK("pack_shade_kernel");
     vis.shade = reinterpret_cast<const int32_t*>(packed);
   }
-  rc = vis_dft_impl(cfg, scale, dlmn, sky, vis, nullptr, viss, ws, p.bytes, st);
+  rc = vis_dft_impl(cfg, scale, dlmn, sky, vis, bt, nullptr, Tuning{}, viss, ws, p.bytes, st,
+                    countLoc ? &map : nullptr);
   if (ws) {
     cudaError_t e = cudaFreeAsync(ws, st);
     if (rc == VISS_OK && e != cudaSuccess) rc = cuda_fail(e, "cudaFreeAsync");
@@ -517,12 +813,15 @@ int viss_imagerecon(int uvw_index, int lmnC_index, int res, float* F, const floa
   viss_vis_set vis{u, v, w, uvwFrequencyMap, nullptr, nullptr, nullptr, uvw_index};
   const double scale[3] = {1.0 / dl, 1.0 / dm, 1.0 / dn};
   const float dlmn[3] = {dl, dm, dn};
+  Batch bt;
+  if ((rc = make_batch(nullptr, uvw_index, cfg, bt))) return rc;
   RecPlan p;
-  plan_recon(p, cfg, uvw_index, lmnC_index, nullptr);
+  plan_recon(p, cfg, bt, lmnC_index, nullptr, Tuning{});
   void* ws = nullptr;
   if (p.bytes) VISS_CUDA(cudaMallocAsync(&ws, p.bytes, st));
   const float* ratios[4] = {thetaP0, phiP0, dtheta, dphi};
-  rc = recon_impl(cfg, scale, dlmn, sky, vis, nullptr, viss, F, ws, p.bytes, st, masked ? ratios : nullptr);
+  rc = recon_impl(cfg, scale, dlmn, sky, vis, bt, nullptr, Tuning{}, viss, F, ws, p.bytes, st,
+                  masked ? ratios : nullptr);
   if (rc == VISS_OK && masked && precision != VISS_PREC_PLAIN) {
     // rows whose ratio arrays are not of the reference's form are rejected
     int flags[2] = {0, 0};
@@ -530,7 +829,7 @@ int viss_imagerecon(int uvw_index, int lmnC_index, int res, float* F, const floa
     cudaError_t e = cudaMemcpyAsync(flags, p.flags, sizeof(flags), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_fail(e, "flag readback");
-    else if (flags[1] & 4) rc = fail(VISS_ERR_UNSUPPORTED, "thetaP0 != dtheta or phiP0 != dphi");
+    else if (flags[FLAG_ERR] & 4) rc = fail(VISS_ERR_UNSUPPORTED, "thetaP0 != dtheta or phiP0 != dphi");
   }
   if (ws) {
     cudaError_t e = cudaFreeAsync(ws, st);

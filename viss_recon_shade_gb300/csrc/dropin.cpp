@@ -9,7 +9,8 @@
 //   MIncline_generate_uvw_float   MIncline_generate_uvw_float.cu:184-484
 //
 // Every constant the reference hard-codes is a flag with the reference's value
-// as default.  Non-identity fine->coarse sky maps are rejected (VISS_ERR_UNSUPPORTED).
+// as default.  Non-identity fine->coarse sky maps average the fine pixels of
+// every coarse pixel, as the reference's visscal does.
 #include <cuda_runtime.h>
 
 #include <chrono>
@@ -136,19 +137,26 @@ int vissgen(const Args& a, bool tenM) {
     return 1;
   }
   l.resize(J); m.resize(J); n.resize(J); FF.resize(X); NX.resize(std::min<size_t>(NX.size(), (size_t)X));
-  // identity fine->coarse map only
-  bool identity = X == J && (int64_t)NX.size() == X;
+  if ((int64_t)NX.size() < X) NX.resize(X, 0.0f);
+  // fine->coarse map: the identity (X == J, NX[i] = i + 1, countLoc = 1) runs on the
+  // coarse brightness directly; any other map averages the fine pixels per coarse
+  // pixel (10M: countLoc.txt / NXq.txt as read, :261-286; 1M: inverted from NX,
+  // vissGen1M_shade_optim1.cu:54-115)
+  std::vector<float> cl;
+  bool identity = X == J;
   for (int64_t i = 0; identity && i < X; ++i) identity = (int64_t)NX[i] == i + 1;
   if (tenM) {
-    std::vector<float> cl;
-    if (read_col(lmn + "countLoc.txt", false, cl) == VISS_OK && read_col(lmn + "NXq.txt", false, NXq) == VISS_OK) {
-      for (int64_t j = 0; identity && j < J && j < (int64_t)cl.size(); ++j) identity = cl[j] == 1.0f;
-      for (int64_t i = 0; identity && i < X && i < (int64_t)NXq.size(); ++i) identity = (int64_t)NXq[i] == i;
+    if (read_col(lmn + "countLoc.txt", false, cl) || read_col(lmn + "NXq.txt", false, NXq)) {
+      std::fprintf(stderr, "cannot read countLoc.txt / NXq.txt under %s: %s\n", lmn.c_str(), viss_last_error());
+      return 1;
     }
-  }
-  if (!identity) {
-    std::fprintf(stderr, "non-identity fine->coarse sky map (NX/countLoc/NXq) is not supported\n");
-    return 2;
+    if ((int64_t)cl.size() < J || (int64_t)NXq.size() < X) {
+      std::fprintf(stderr, "countLoc.txt / NXq.txt shorter than the sky\n");
+      return 1;
+    }
+    cl.resize(J); NXq.resize(X);
+    for (int64_t j = 0; identity && j < J; ++j) identity = cl[j] == 1.0f;
+    for (int64_t i = 0; identity && i < X; ++i) identity = (int64_t)NXq[i] == i;
   }
   for (auto& x : n) x = std::fmax(-1.0f, std::fmin(1.0f, x));  // clip_functor (:308)
 
@@ -169,10 +177,31 @@ int vissgen(const Args& a, bool tenM) {
     }
   }
 
-  Dev<float> dl_, dm_, dn_, dFF;
-  if (dl_.up(l.data(), J) || dm_.up(m.data(), J) || dn_.up(n.data(), J) || dFF.up(FF.data(), J)) {
+  Dev<float> dl_, dm_, dn_, dFF, dNXqf;
+  Dev<int32_t> dcl, dNXqi;
+  if (dl_.up(l.data(), J) || dm_.up(m.data(), J) || dn_.up(n.data(), J) || dFF.up(FF.data(), identity ? J : X)) {
     std::fprintf(stderr, "device allocation failed\n");
     return 1;
+  }
+  if (!identity) {
+    if (tenM) {
+      std::vector<int32_t> cli(J);
+      for (int64_t j = 0; j < J; ++j) cli[j] = (int32_t)cl[j];
+      if (dcl.up(cli.data(), J) || dNXqf.up(NXq.data(), X)) {
+        std::fprintf(stderr, "device allocation failed\n");
+        return 1;
+      }
+    } else {
+      Dev<float> dNX;
+      Dev<char> ws;
+      const size_t nb = viss_nxq_workspace(X, J);
+      if (dNX.up(NX.data(), X) || dcl.alloc(J) || dNXqi.alloc(X) || ws.alloc(nb)) {
+        std::fprintf(stderr, "device allocation failed\n");
+        return 1;
+      }
+      CHECKV(viss_nxq(dNX.p, X, J, dcl.p, dNXqi.p, ws.p, nb, nullptr));
+      CHECKC(cudaDeviceSynchronize());
+    }
   }
   const std::string outdir = tenM ? root + "/F_recon_10M/" : root + "/F_recon_1M/";
   mkdir_p(outdir);
@@ -225,8 +254,33 @@ int vissgen(const Args& a, bool tenM) {
     }
     const double t1 = now();
     const int var = variant == "plain" ? VISS_VARIANT_PLAIN : VISS_VARIANT_OPTIM;
-    CHECKV(viss_visscal((int)K, (int)J, RES, dFF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dM1.p, dM2.p, dM3.p,
-                        dM4.p, nullptr, nullptr, d, d, d, var, mask, precision, nullptr));
+    if (identity || tenM) {
+      CHECKV(viss_visscal((int)K, (int)J, RES, dFF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dM1.p, dM2.p,
+                          dM3.p, dM4.p, identity ? nullptr : dNXqf.p, identity ? nullptr : dcl.p, d, d, d, var, mask,
+                          precision, nullptr));
+    } else {
+      // 1M with the in-program int NXq: the general map entry point with visscal's conventions
+      viss_dft_cfg cfg{};
+      cfg.mask_mode = mask; cfg.recon_mask = VISS_RECON_MASK_NONE; cfg.precision = precision; cfg.res = RES;
+      cfg.trunc_brightness = var == VISS_VARIANT_PLAIN; cfg.occluded_value = 240.0f; cfg.phase_scale = 1.0 / d;
+      cfg.n_offset = 0.0; cfg.moon_radius_km = 1737.4; cfg.norm = 1.0;
+      std::vector<int32_t> sh(4 * (size_t)K);
+      for (int64_t k = 0; k < K; ++k) {
+        sh[4 * k] = M1[k]; sh[4 * k + 1] = M2[k]; sh[4 * k + 2] = M3[k]; sh[4 * k + 3] = M4[k];
+      }
+      Dev<int32_t> dsh;
+      Dev<char> ws;
+      viss_sky sky{dl_.p, dm_.p, dn_.p, nullptr, J};
+      viss_fine_map fm{dFF.p, nullptr, dNXqi.p, dcl.p, X};
+      viss_vis_set vs{du.p, dv.p, dw.p, nullptr, nullptr, nullptr, nullptr, K};
+      const size_t nb = viss_vis_dft_map_workspace(&cfg, K, J, &fm, nullptr);
+      if (dsh.up(sh.data(), 4 * K) || ws.alloc(nb)) {
+        std::fprintf(stderr, "device allocation failed\n");
+        return 1;
+      }
+      vs.shade = dsh.p;
+      CHECKV(viss_vis_dft_map(&cfg, &sky, &fm, &vs, nullptr, dV.p, ws.p, nb, nullptr));
+    }
     CHECKC(cudaDeviceSynchronize());
     const double t2 = now();
     CHECKV(viss_imagerecon((int)K, (int)J, RES, dF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dwgt.p, dr1.p,

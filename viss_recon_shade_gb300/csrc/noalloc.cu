@@ -26,10 +26,6 @@ namespace viss {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VISS_NOALLOC_SCRATCH_BYTES];
 
-int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
-                 const viss_vis_set& vis, const viss_geometry* geo, float* V, void* ws, size_t ws_bytes,
-                 cudaStream_t st);
-
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;

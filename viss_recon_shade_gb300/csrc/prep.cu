@@ -124,41 +124,68 @@ __device__ int recon_ratio_tmax(float r) {
   return 0;
 }
 
+// Input row of padded row pr, or -1 for a padding row.
+__device__ __forceinline__ int64_t padded_row_source(const ChannelRows& ch, int64_t pr) {
+  const int64_t b = pr / VIS_ROWS;
+  int lo = 0, hi = ch.nch - 1;  // channel c with rb_off[c] <= b < rb_off[c+1]
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ch.rb_off[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  const int64_t k = ch.row_off[lo] + (pr - ch.rb_off[lo] * VIS_ROWS);
+  return k < ch.row_off[lo + 1] ? k : -1;
+}
+
 __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.Kpad) return;
-  if (k >= a.K) {
-    a.rec0[k] = make_int4(0, 0, 0, 0);
-    a.rec1[k] = make_int4(0, 0, 0, PHASE_BIAS);
-    if (a.uf) a.uf[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a.win) a.win[k] = make_int4(1, 0, 0, 0);
-    if (a.y) a.y[k] = make_float2(0.f, 0.f);
+  const int64_t pr = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pr >= a.Kpad) return;
+  const int64_t k = a.padded ? padded_row_source(a.ch, pr) : (pr < a.K ? pr : -1);
+  if (k < 0) {
+    a.rows0[pr] = make_int4(0, 0, 0, PHASE_BIAS);
+    a.rows1[pr] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.rowsat) a.rowsat[pr] = PAD_PACKED;
+    if (a.uf) a.uf[pr] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.win) a.win[pr] = recon ? make_int4(0, 0, 0, 0) : make_int4(1, 0, 0, 0);
     return;
   }
   const double uu = a.u[k], vv = a.v[k], ww = a.w[k];
   const double Uu = floor(uu + 0.5), Uv = floor(vv + 0.5), Uw = floor(ww + 0.5);
   const double lim = 1073741824.0;  // |U| < 2^30
-  if (!(fabs(Uu) < lim && fabs(Uv) < lim && fabs(Uw) < lim)) atomicOr(a.flags + 1, 1);
+  if (!(fabs(Uu) < lim && fabs(Uv) < lim && fabs(Uw) < lim)) atomicOr(a.flags + FLAG_ERR, 1);
   const double fu = uu - Uu, fv = vv - Uv, fw = ww - Uw;  // exact, in [-1/2, 1/2)
-  if (fu != 0.0 || fv != 0.0 || fw != 0.0) atomicOr(a.flags, 1);
-  int packed = 0;
-  if (a.snap && a.pair) {
+  if (fu != 0.0 || fv != 0.0 || fw != 0.0) atomicOr(a.flags + FLAG_FRAC, 1);
+  if (a.rowsat) {
+    int packed = PAD_PACKED;
     const int s = a.snap[k];
-    const int pr = a.pair[k];
-    const int pm = pr & 0xffff, pn = (pr >> 16) & 0xffff;
-    if (s < 0 || s >= a.S || pm >= a.nsat || pn >= a.nsat) {
-      atomicOr(a.flags + 1, 2);
-    } else {
-      packed = (s * a.nsat + pm) | ((pn - pm + 32) << 26);
+    const int pr2 = a.pair[k];
+    const int pm = pr2 & 0xffff, pn = (pr2 >> 16) & 0xffff;
+    if (s < 0 || s >= a.S || pm >= a.nsat || pn >= a.nsat) atomicOr(a.flags + FLAG_ERR, 2);
+    else packed = (s * a.nsat + pm) | ((pn - pm + 32) << 26);
+    a.rowsat[pr] = packed;
+  }
+  // PHASE_BIAS plus the per-row part of f_w * z: f_w * sn * n_offset; the
+  // reconstruction folds the visibility's phase in too: y e^{ix} = |y| e^{i(x + arg y)}
+  uint32_t bias = (uint32_t)PHASE_BIAS + fix32(fw * a.sn * a.n_offset);
+  float c = 0.f;
+  if (recon) {
+    const double wg = a.wgt ? (double)a.wgt[k] : 1.0;
+    const double yr = wg * (double)a.V[2 * k], yi = wg * (double)a.V[2 * k + 1];
+    c = (float)sqrt(yr * yr + yi * yi);
+    if (c > 0.f) bias += fix32(atan2(yi, yr) * (0.5 / kPi));
+    // every other row: half a turn more and -|y| (the same term), so that a
+    // systematic error of the SFU's sin/cos cancels over the rows instead of
+    // adding up with the all-positive weights |y|
+    if (k & 1) {
+      bias += 0x80000000u;
+      c = -c;
     }
   }
-  // PHASE_BIAS plus the per-row part of f_w * z: f_w * sn * n_offset
-  const int bias = (int)((uint32_t)PHASE_BIAS + fix32(fw * a.sn * a.n_offset));
-  a.rec0[k] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, packed);
-  a.rec1[k] = make_int4(__float_as_int((float)fu), __float_as_int((float)fv), __float_as_int((float)fw), bias);
-  if (a.uf) a.uf[k] = make_float4((float)Uu, (float)Uv, (float)Uw, 0.f);
+  a.rows0[pr] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, (int)bias);
+  a.rows1[pr] = make_float4((float)fu, (float)fv, (float)fw, c);
+  if (a.uf) a.uf[pr] = make_float4((float)Uu, (float)Uv, (float)Uw, 0.f);
   if (a.win) {
-    int4 wv = make_int4(1, 0, 0, 0);  // empty
+    int4 wv = recon ? make_int4(0, 0, 0, 0) : make_int4(1, 0, 0, 0);  // empty
     if (a.shade) {
       const int M1 = a.shade[4 * k], M2 = a.shade[4 * k + 1], M3 = a.shade[4 * k + 2],
                 M4 = a.shade[4 * k + 3];
@@ -173,11 +200,7 @@ __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
         wv = make_int4(recon_ratio_tmax(r1), recon_ratio_tmax(r2), 0, 0);
       }
     }
-    a.win[k] = wv;
-  }
-  if (a.y) {
-    const float wg = a.wgt ? a.wgt[k] : 1.0f;
-    a.y[k] = make_float2(wg * a.V[2 * k], wg * a.V[2 * k + 1]);
+    a.win[pr] = wv;
   }
 }
 
@@ -307,29 +330,29 @@ __device__ void cone_block(const float4* satdir, int64_t count, Member member, f
 }
 
 struct RowMember {
-  const int4* rows0;
-  const int4* rows1;
+  const int* rowsat;
   int64_t base;
   __device__ int operator()(int64_t i) const {
-    const int p = rows0[base + (i >> 1)].w;
+    const int p = rowsat[base + (i >> 1)];
     return (i & 1) ? sat_gn(p) : sat_gm(p);
   }
 };
 
-__global__ void rowblock_cones_kernel(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
-                                      int rows_per_block, float4* cones) {
+// One cone per padded block of VIS_ROWS rows, over the block's real rows.
+__global__ void rowblock_cones_kernel(const int* rowsat, const float4* satdir, const ChannelRows ch, float4* cones) {
   const int64_t b = blockIdx.x;
-  const int64_t base = b * rows_per_block;
-  int64_t cnt = K - base;
-  if (cnt > rows_per_block) cnt = rows_per_block;
+  int c = 0;
+  while (c + 1 < ch.nch && b >= ch.rb_off[c + 1]) ++c;
+  int64_t cnt = (ch.row_off[c + 1] - ch.row_off[c]) - (b - ch.rb_off[c]) * VIS_ROWS;
+  if (cnt > VIS_ROWS) cnt = VIS_ROWS;
   if (cnt < 0) cnt = 0;
-  cone_block(satdir, 2 * cnt, RowMember{rows0, rows1, base}, cones + 2 * b);
+  cone_block(satdir, 2 * cnt, RowMember{rowsat, b * VIS_ROWS}, cones + 2 * b);
 }
 
-int launch_prep_rowblock_cones(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
-                               int rows_per_block, int64_t nblocks, float4* cones, cudaStream_t st) {
+int launch_prep_rowblock_cones(const int* rowsat, const float4* satdir, const ChannelRows& ch, int64_t nblocks,
+                               float4* cones, cudaStream_t st) {
   if (nblocks <= 0) return VISS_OK;
-  rowblock_cones_kernel<<<(unsigned)nblocks, 256, 0, st>>>(rows0, rows1, satdir, K, rows_per_block, cones);
+  rowblock_cones_kernel<<<(unsigned)nblocks, 256, 0, st>>>(rowsat, satdir, ch, cones);
   VISS_LAUNCH_CHECK("rowblock_cones_kernel");
   return VISS_OK;
 }

@@ -3,10 +3,12 @@
 //
 // F_j = norm * sum_k [not masked] y_k exp(+2 pi i t_kj),  y_k = wgt_k V_k
 //
-// A CTA owns REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates in
-// registers) and streams visibility records (uvw fixed point + y) through
-// shared memory in tiles of REC_Q.  Per term: 3 IMAD [+fractional, +compensated
-// terms as in the vis kernel], turns -> angle, __sincosf, 4 FFMA.
+// A work item is REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates
+// in registers) against one segment of visibility rows of one channel, streamed
+// through shared memory in tiles of REC_Q.  The phase of y_k is folded into the
+// row's fixed-point bias (y e^{ix} = |y| e^{i(x + arg y)}), so a term is the
+// same as in the vis kernel: 3 IMAD [+4 FFMA fractional uvw] [+3 FFMA
+// compensated], turns -> angle, __sincosf, 2 FFMA with |y_k|.
 // Masks:
 //   GEOMETRIC: rows come in snapshot runs; per run every thread tests its pixels
 //     against the snapshot's bounding cone and the warp votes: all occluded ->
@@ -14,8 +16,10 @@
 //     per-pixel satellite occlusion bitmask and tests each row's pair.
 //   REF: the reference ratio mask can only fire on pixels (thetaP, phiP) with
 //     1 <= thetaP <= tmax_k, 1 <= phiP <= pmax_k; tiles whose rows cannot touch
-//     the CTA's pixels run unmasked.
-// Visibility chunks (blockIdx.y) give partial sums, reduced in a fixed order.
+//     the item's pixels run unmasked.
+// Persistent CTAs take items from an atomic counter, longest segments first.
+// A channel split into several segments leaves partial sums per segment,
+// reduced in a fixed order.
 #include "viss_internal.cuh"
 
 namespace viss {
@@ -26,25 +30,22 @@ __device__ __noinline__ bool geo_exact_pix(const ReconParams& p, int j, int gidx
 }
 
 template <bool FRAC, bool COMP>
-__device__ __forceinline__ void rec_term(const int4& r0, const int4& r1, const float4& rf, float2 y, int A, int B,
+__device__ __forceinline__ void rec_term(const int4& r0, const float4& r1, const float4& rf, float c, int A, int B,
                                          int C, float X, float Y, float Z, float lx, float ly, float lz, float& fr,
                                          float& fi) {
-  uint32_t q = (uint32_t)r0.x * (uint32_t)A + (uint32_t)r0.y * (uint32_t)B + (uint32_t)r0.z * (uint32_t)C +
-               (uint32_t)(FRAC ? r1.w : PHASE_BIAS);
-  float delta = 0.f;
-  if (FRAC) delta = fmaf(__int_as_float(r1.x), X, fmaf(__int_as_float(r1.y), Y, __int_as_float(r1.z) * Z));
-  if (FRAC && !COMP) q += frac_phase(delta);
+  const uint32_t q = (uint32_t)r0.x * (uint32_t)A + (uint32_t)r0.y * (uint32_t)B + (uint32_t)r0.z * (uint32_t)C +
+                     (uint32_t)r0.w;
   float x = turns_to_angle(q);
-  if (COMP) {
-    const float d = fmaf(rf.x, lx, fmaf(rf.y, ly, fmaf(rf.z, lz, delta)));
+  if (FRAC || COMP) {
+    float d = 0.f;
+    if (FRAC) d = fmaf(r1.x, X, fmaf(r1.y, Y, r1.z * Z));
+    if (COMP) d = fmaf(rf.x, lx, fmaf(rf.y, ly, fmaf(rf.z, lz, d)));
     x = fmaf(d, K2PI, x);
   }
   float sn, cs;
   __sincosf(x, &sn, &cs);
-  fr = fmaf(y.x, cs, fr);
-  fr = fmaf(-y.y, sn, fr);
-  fi = fmaf(y.x, sn, fi);
-  fi = fmaf(y.y, cs, fi);
+  fr = fmaf(c, cs, fr);
+  fi = fmaf(c, sn, fi);
 }
 
 constexpr int RM_NONE = 0, RM_REF = 1, RM_GEO = 2;
@@ -54,10 +55,10 @@ constexpr int REC_CONE_CACHE = 128;  // snapshot cones cached per tile
 template <int RM, bool COMP>
 struct RecSmem {
   int4 r0[REC_Q];
-  int4 r1[REC_Q];
+  float4 r1[REC_Q];
   float4 rf[COMP ? REC_Q : 1];
-  float2 y[REC_Q];
   int4 win[RM == RM_REF ? REC_Q : 1];
+  int pk[RM == RM_GEO ? REC_Q : 1];
   int snap[RM == RM_GEO ? REC_Q : 1];
   int runend[RM == RM_GEO ? REC_Q : 1];
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
@@ -67,11 +68,12 @@ struct RecSmem {
 };
 
 template <int RM, bool FRAC, bool COMP>
-__device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm) {
+__device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm, int64_t pb, int64_t kb,
+                                           int64_t ke, float2* out, float norm, bool direct) {
   const int tid = threadIdx.x;
   // a warp owns 32 * REC_TJ consecutive positions: with the spatial order of
   // the geometric passes that is one compact patch of sky
-  const int64_t j0 = (int64_t)blockIdx.x * REC_PIX + (int64_t)tid * REC_TJ;
+  const int64_t j0 = pb * REC_PIX + (int64_t)tid * REC_TJ;
   int A[REC_TJ], B[REC_TJ], C[REC_TJ];
   float XF[REC_TJ], YF[REC_TJ], ZF[REC_TJ];
   float LX[REC_TJ], LY[REC_TJ], LZ[REC_TJ];
@@ -96,10 +98,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
   bool valid[REC_TJ];
 #pragma unroll
   for (int i = 0; i < REC_TJ; ++i) valid[i] = j0 + i < p.J;
-  const int64_t kb = (int64_t)blockIdx.y * p.kchunk;
-  int64_t ke = kb + p.kchunk;
-  if (ke > p.K) ke = p.K;
-  const int64_t jfirst = (int64_t)blockIdx.x * REC_PIX;
+  const int64_t jfirst = pb * REC_PIX;
   int64_t jlast = jfirst + REC_PIX - 1;
   if (jlast > p.J - 1) jlast = p.J - 1;
 
@@ -111,11 +110,9 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     bool hit = false;
     for (int r = tid; r < nq; r += REC_THREADS) {
       const int64_t k = tile + r;
-      const int4 r0 = p.rows0[k];
-      sm.r0[r] = r0;
-      if (FRAC) sm.r1[r] = p.rows1[k];
+      sm.r0[r] = p.rows0[k];
+      sm.r1[r] = p.rows1[k];
       if (COMP) sm.rf[r] = p.rowsf[k];
-      sm.y[r] = p.y[k];
       if (RM == RM_REF) {
         const int4 wv = p.win[k];
         sm.win[r] = wv;
@@ -125,7 +122,9 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         }
       }
       if (RM == RM_GEO) {
-        const int sn = sat_gm(r0.w) / p.nsat;
+        const int pk = p.rowsat[k];
+        const int sn = sat_gm(pk) / p.nsat;
+        sm.pk[r] = pk;
         sm.snap[r] = sn;
         atomicMin(&sm.srange[0], sn);
         atomicMax(&sm.srange[1], sn);
@@ -172,14 +171,12 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
 #pragma unroll 2
           for (int rr = r; rr < re; ++rr) {
             const int4 r0 = sm.r0[rr];
-            int4 r1 = make_int4(0, 0, 0, 0);
+            const float4 r1 = sm.r1[rr];
             float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (FRAC) r1 = sm.r1[rr];
             if (COMP) rf = sm.rf[rr];
-            const float2 y = sm.y[rr];
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i)
-              rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
+              rec_term<FRAC, COMP>(r0, r1, rf, r1.w, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
                                    tr[i], ti[i]);
           }
         } else {
@@ -201,16 +198,15 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
           }
           for (int rr = r; rr < re; ++rr) {
             const int4 r0 = sm.r0[rr];
-            int4 r1 = make_int4(0, 0, 0, 0);
-            if (FRAC) r1 = sm.r1[rr];
+            const float4 r1 = sm.r1[rr];
             float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
             if (COMP) rf = sm.rf[rr];
-            const float2 y = sm.y[rr];
-            const uint32_t pm = (1u << (sat_gm(r0.w) - g0)) | (1u << (sat_gn(r0.w) - g0));
+            const int pk = sm.pk[rr];
+            const uint32_t pm = (1u << (sat_gm(pk) - g0)) | (1u << (sat_gn(pk) - g0));
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i) {
-              const float2 yy = (bits[i] & pm) ? make_float2(0.f, 0.f) : y;
-              rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
+              const float c = (bits[i] & pm) ? 0.f : r1.w;
+              rec_term<FRAC, COMP>(r0, r1, rf, c, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i],
                                    tr[i], ti[i]);
             }
           }
@@ -220,17 +216,15 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     } else if (RM == RM_REF && masked_tile) {
       for (int rr = 0; rr < nq; ++rr) {
         const int4 r0 = sm.r0[rr];
-        int4 r1 = make_int4(0, 0, 0, 0);
+        const float4 r1 = sm.r1[rr];
         float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (FRAC) r1 = sm.r1[rr];
         if (COMP) rf = sm.rf[rr];
-        const float2 y = sm.y[rr];
         const int4 wv = sm.win[rr];
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i) {
           const bool skip = TP[i] >= 1 && TP[i] <= wv.x && PP[i] >= 1 && PP[i] <= wv.y;
-          const float2 yy = skip ? make_float2(0.f, 0.f) : y;
-          rec_term<FRAC, COMP>(r0, r1, rf, yy, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
+          const float c = skip ? 0.f : r1.w;
+          rec_term<FRAC, COMP>(r0, r1, rf, c, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
                                ti[i]);
         }
       }
@@ -238,14 +232,12 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
 #pragma unroll 2
       for (int rr = 0; rr < nq; ++rr) {
         const int4 r0 = sm.r0[rr];
-        int4 r1 = make_int4(0, 0, 0, 0);
+        const float4 r1 = sm.r1[rr];
         float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (FRAC) r1 = sm.r1[rr];
         if (COMP) rf = sm.rf[rr];
-        const float2 y = sm.y[rr];
 #pragma unroll
         for (int i = 0; i < REC_TJ; ++i)
-          rec_term<FRAC, COMP>(r0, r1, rf, y, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
+          rec_term<FRAC, COMP>(r0, r1, rf, r1.w, A[i], B[i], C[i], XF[i], YF[i], ZF[i], LX[i], LY[i], LZ[i], tr[i],
                                ti[i]);
       }
     }
@@ -264,59 +256,82 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     const float4 t = sm.acc[tid * REC_TJ + i];
     const float fr = t.x, fi = t.y;
     if (pos < p.J) {
-      if (p.nsplit == 1) {
+      if (direct) {
         const int64_t j = p.perm ? (int64_t)p.perm[pos] : pos;
-        p.out[j] = make_float2(-fr * p.norm, -fi * p.norm);
+        out[j] = make_float2(-fr * norm, -fi * norm);
       } else {
-        p.out[(int64_t)blockIdx.y * p.J + pos] = make_float2(fr, fi);
+        out[pos] = make_float2(fr, fi);
       }
     }
   }
 }
 
+// Persistent: grid = resident CTAs; each CTA takes the next work item (segment,
+// pixel block) from an atomic counter until none are left.  The counter is
+// reset by the host before the launch; no CTA waits on another.
 template <int RM, bool COMP>
 __global__ void __launch_bounds__(REC_THREADS, VISS_REC_MINB) recon_fast_kernel(const ReconParams p) {
   __shared__ RecSmem<RM, COMP> sm;
-  if (__ldg(p.flags) != 0) recon_body<RM, true, COMP>(p, sm);
-  else recon_body<RM, false, COMP>(p, sm);
+  __shared__ int s_item;
+  const bool frac = __ldg(p.flags + FLAG_FRAC) != 0;
+  for (;;) {
+    __syncthreads();  // everyone has read the previous item
+    if (threadIdx.x == 0) s_item = atomicAdd(p.flags + FLAG_REC_COUNTER, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= p.nitems) break;
+    const int seg = item / p.npb;
+    const int64_t pb = item - (int64_t)seg * p.npb;
+    const int ch = p.seg_ch[seg], slot = p.seg_slot[seg];
+    const bool direct = slot < 0;
+    float2* out = direct ? p.out + (int64_t)ch * p.J : p.partial + (int64_t)slot * p.J;
+    if (frac) recon_body<RM, true, COMP>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
+    else recon_body<RM, false, COMP>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
+  }
 }
 
 template <int RM>
-static void launch_rm(const ReconParams& p, dim3 grid, bool comp, cudaStream_t st) {
-  if (comp) recon_fast_kernel<RM, true><<<grid, REC_THREADS, 0, st>>>(p);
-  else recon_fast_kernel<RM, false><<<grid, REC_THREADS, 0, st>>>(p);
+static void launch_rm(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
+  if (comp) {
+    const int g = persistent_grid(recon_fast_kernel<RM, true>, REC_THREADS, ctas_per_sm, p.nitems);
+    recon_fast_kernel<RM, true><<<g, REC_THREADS, 0, st>>>(p);
+  } else {
+    const int g = persistent_grid(recon_fast_kernel<RM, false>, REC_THREADS, ctas_per_sm, p.nitems);
+    recon_fast_kernel<RM, false><<<g, REC_THREADS, 0, st>>>(p);
+  }
 }
 
-int launch_recon_fast(const ReconParams& p, int64_t npb, bool comp, cudaStream_t st) {
-  const dim3 grid((unsigned)npb, (unsigned)p.nsplit);
+int launch_recon_fast(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
+  if (p.nitems <= 0) return VISS_OK;
   switch (p.recon_mask) {
-    case VISS_RECON_MASK_NONE: launch_rm<RM_NONE>(p, grid, comp, st); break;
-    case VISS_RECON_MASK_REF: launch_rm<RM_REF>(p, grid, comp, st); break;
-    case VISS_RECON_MASK_GEOMETRIC: launch_rm<RM_GEO>(p, grid, comp, st); break;
+    case VISS_RECON_MASK_NONE: launch_rm<RM_NONE>(p, ctas_per_sm, comp, st); break;
+    case VISS_RECON_MASK_REF: launch_rm<RM_REF>(p, ctas_per_sm, comp, st); break;
+    case VISS_RECON_MASK_GEOMETRIC: launch_rm<RM_GEO>(p, ctas_per_sm, comp, st); break;
     default: return fail(VISS_ERR_INVALID, "unknown recon mask");
   }
   VISS_LAUNCH_CHECK("recon_fast_kernel");
   return VISS_OK;
 }
 
-__global__ void recon_reduce_kernel(const float2* __restrict__ part, int nsplit, int64_t J, float norm,
-                                    const int32_t* perm, float2* out) {
+// F[c] = norm_c * -(sum of channel c's partial slots), slots summed in order in double.
+__global__ void recon_reduce_kernel(const RecReduceParams p) {
   const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (pos >= J) return;
+  const int c = blockIdx.y;
+  if (pos >= p.J || p.nslot[c] == 0) return;
   double sr = 0.0, si = 0.0;
-  for (int s = 0; s < nsplit; ++s) {
-    const float2 v = part[(int64_t)s * J + pos];
+  for (int s = 0; s < p.nslot[c]; ++s) {
+    const float2 v = p.partial[(int64_t)(p.slot0[c] + s) * p.J + pos];
     sr += v.x;
     si += v.y;
   }
-  const int64_t j = perm ? (int64_t)perm[pos] : pos;
-  out[j] = make_float2((float)(-sr * norm), (float)(-si * norm));
+  const int64_t j = p.perm ? (int64_t)p.perm[pos] : pos;
+  const double norm = p.norm[c];
+  p.out[(int64_t)c * p.J + j] = make_float2((float)(-sr * norm), (float)(-si * norm));
 }
 
-int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, const int32_t* perm, float2* out,
-                        cudaStream_t st) {
-  if (J <= 0) return VISS_OK;
-  recon_reduce_kernel<<<(unsigned)((J + 255) / 256), 256, 0, st>>>(partial, nsplit, J, norm, perm, out);
+int launch_recon_reduce(const RecReduceParams& p, cudaStream_t st) {
+  if (p.J <= 0 || p.nch <= 0) return VISS_OK;
+  recon_reduce_kernel<<<dim3((unsigned)((p.J + 255) / 256), (unsigned)p.nch), 256, 0, st>>>(p);
   VISS_LAUNCH_CHECK("recon_reduce_kernel");
   return VISS_OK;
 }

@@ -2,12 +2,13 @@
 //
 // V_k = sum_j C_kj exp(-2 pi i t_kj),  t_kj = s (u_k l_j + v_k m_j + w_k (n_j + n_offset))
 //
-// Tiled kernel: a CTA owns VIS_ROWS = 1024 visibilities (4 per thread, in
-// registers) and streams the sky through shared memory in tiles of VIS_P
-// pixels; every thread reads each pixel record as a broadcast.  Per term:
+// Tiled kernel: a work item is VIS_ROWS = 1024 visibilities of one channel (4
+// per thread, in registers) against one chunk of the sky, streamed through
+// shared memory in tiles of VIS_P pixels; every thread reads each pixel record
+// as a broadcast.  Per term:
 //   3 IMAD (phase mod 1 turn in 32-bit fixed point; exact for integer uvw)
-//   [+3 IMAD.HI +1 LEA for fractional uvw] [+4 FFMA compensation]
-//   1 LOP/LEA + 1 FFMA (turns -> angle), __sincosf (2 SFU ops), 2 FFMA (MAC).
+//   [+4 FFMA for fractional uvw] [+3 FFMA compensation]
+//   shift/or + 1 FFMA (turns -> angle), __sincosf (2 SFU ops), 2 FFMA (MAC).
 // The occlusion predicate is evaluated inline per tile:
 //   GEOMETRIC: pixels are classified against a cone bounding the shadow cones
 //     of every satellite used by the CTA's rows -- all visible / all occluded /
@@ -16,7 +17,7 @@
 //     satellites, decided in double within GEO_EPS of the limb).
 //   REF_*: per-row window (row range x column range on the fine grid); tiles
 //     no window of the CTA touches run the unmasked loop.
-// Pixel chunks (blockIdx.y) give partial sums, reduced in a fixed order.
+// Pixel chunks give partial sums, reduced in a fixed order.
 #include "viss_internal.cuh"
 
 namespace viss {
@@ -25,15 +26,14 @@ template <bool FRAC, bool COMP>
 __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const float4& lo, float c, int U,
                                          int V, int W, float FU, float FV, float FW, int bias, float UF, float VF,
                                          float WF, float& ar, float& ai) {
-  uint32_t q = (uint32_t)U * (uint32_t)a.x + (uint32_t)V * (uint32_t)a.y + (uint32_t)W * (uint32_t)a.z +
-               (uint32_t)(FRAC ? bias : PHASE_BIAS);
-  float delta = 0.f;
-  if (FRAC) delta = fmaf(FU, __int_as_float(b.x), fmaf(FV, __int_as_float(b.y), FW * __int_as_float(b.z)));
-  if (FRAC && !COMP) q += frac_phase(delta);
+  const uint32_t q = (uint32_t)U * (uint32_t)a.x + (uint32_t)V * (uint32_t)a.y + (uint32_t)W * (uint32_t)a.z +
+                     (uint32_t)bias;
   float x = turns_to_angle(q);
-  if (COMP) {
-    // fractional part and the pixel fixed-point rounding, in FP32, added to the angle
-    const float d = fmaf(UF, lo.x, fmaf(VF, lo.y, fmaf(WF, lo.z, delta)));
+  if (FRAC || COMP) {
+    // fractional uvw [and the pixel fixed-point rounding], in FP32, added to the angle
+    float d = 0.f;
+    if (FRAC) d = fmaf(FU, __int_as_float(b.x), fmaf(FV, __int_as_float(b.y), FW * __int_as_float(b.z)));
+    if (COMP) d = fmaf(UF, lo.x, fmaf(VF, lo.y, fmaf(WF, lo.z, d)));
     x = fmaf(d, K2PI, x);
   }
   float sn, cs;
@@ -76,6 +76,46 @@ __device__ __noinline__ bool ref_hit_general(int4 wv, int64_t j, int res) {
   return lo_min <= lo_max;
 }
 
+// Fine->coarse map: pixel j's value for window wv, exactly as the reference's
+// member loop (mean over its fine members, the occluded value inside the window).
+__device__ __noinline__ float ref_members_value(const FineMapDev& m, int4 wv, int64_t j, int res, float occ) {
+  const int2 mm = m.mem[j];
+  double sum = 0.0;
+  for (int c = 0; c < mm.y; ++c) {
+    const int i = m.members[mm.x + c];
+    if (i < 0) {  // rejected index (flagged in the prep)
+      sum = nan("");
+      continue;
+    }
+    float ff = m.FF[i];
+    if (m.trunc) ff = (float)(int)ff;
+    bool hit = false;
+    if (wv.x <= wv.y) {
+      if (wv.z + 1 >= 0 && wv.w <= res) {
+        const int q = i / res, r = i - q * res;
+        hit = q >= wv.x && q <= wv.y && r > wv.z && r < wv.w;
+      } else {
+        hit = ref_hit_general(wv, i, res);
+      }
+    }
+    sum += hit ? (double)occ : (double)ff;
+  }
+  return (float)(sum / (double)mm.y);  // 0/0 = NaN for an empty pixel, as the reference
+}
+
+// Fine->coarse map: the pixel's bounding box of members decides most terms
+// (disjoint from the window: base brightness c0; inside it: occ); the rest
+// take the exact member loop.
+__device__ __forceinline__ float ref_map_value(const FineMapDev& m, const int4& wv, const int4& bx, float c0, float occ,
+                                               int64_t j, int res) {
+  if (wv.x > wv.y) return c0;
+  if (wv.z + 1 >= 0 && wv.w <= res) {
+    if (bx.y < wv.x || bx.x > wv.y || bx.w <= wv.z || bx.z >= wv.w) return c0;
+    if (bx.x >= wv.x && bx.y <= wv.y && bx.z > wv.z && bx.w < wv.w) return occ;
+  }
+  return ref_members_value(m, wv, j, res, occ);
+}
+
 template <int MASK, bool COMP>
 struct VisSmem {
   static constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
@@ -91,7 +131,8 @@ struct VisSmem {
 };
 
 template <int MASK, bool FRAC, bool COMP>
-__device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>& sm) {
+__device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>& sm, int64_t rb, int split, int ch,
+                                         int64_t rb_first, int64_t row_first, int64_t nvalid) {
   constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
   constexpr bool REF = MASK == VISS_MASK_REF_QUIRK || MASK == VISS_MASK_REF_INTENDED;
   int4* const s_p0 = sm.p0;
@@ -102,8 +143,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   auto& s_wcnt = sm.wcnt;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int64_t row0 = (int64_t)blockIdx.x * VIS_ROWS;
-  const int split = blockIdx.y;
+  const int64_t row0 = rb * VIS_ROWS;                   // padded row of this rowblock
+  const int64_t local0 = (rb - rb_first) * VIS_ROWS;    // its first row within the channel
+  const float* bright = p.bright ? p.bright + (int64_t)ch * p.J : nullptr;
 
   // Registers per visibility: fixed-point U,V,W [+ fractional F] [+ float U for
   // the compensation] and the two accumulators.  Satellite indices (geometric)
@@ -117,12 +159,11 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   for (int i = 0; i < VIS_TK; ++i) {
     const int64_t k = row0 + tid + i * VIS_THREADS;  // rows are padded to a whole block
     const int4 r0 = p.rows0[k];
-    U[i] = r0.x; V[i] = r0.y; W[i] = r0.z;
+    U[i] = r0.x; V[i] = r0.y; W[i] = r0.z; BI[i] = r0.w;
     FU[i] = FV[i] = FW[i] = 0.f;
-    BI[i] = PHASE_BIAS;
     if (FRAC) {
-      const int4 r1 = p.rows1[k];
-      FU[i] = __int_as_float(r1.x); FV[i] = __int_as_float(r1.y); FW[i] = __int_as_float(r1.z); BI[i] = r1.w;
+      const float4 r1 = p.rows1[k];
+      FU[i] = r1.x; FV[i] = r1.y; FW[i] = r1.z;
     }
     UF[i] = VF[i] = WF[i] = 0.f;
     if (COMP) {
@@ -138,8 +179,8 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   }
   float4 cone0 = make_float4(0.f, 0.f, 0.f, 2.f), cone1 = make_float4(-2.f, 0.f, 0.f, 0.f);
   if (GEO) {
-    cone0 = p.cones[2 * blockIdx.x];
-    cone1 = p.cones[2 * blockIdx.x + 1];
+    cone0 = p.cones[2 * rb];
+    cone1 = p.cones[2 * rb + 1];
   }
   const float occ_val = p.occ_val;
 
@@ -195,6 +236,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         if (c) {
           const int64_t j = tile + tid + qq * VIS_THREADS;
           int4 a = p.pix0[j];
+          if (bright) a.w = __float_as_int(bright[j]);
           const float4 g = p.pgeo[j];
           const float d = fmaf(g.x, cone0.x, fmaf(g.y, cone0.y, g.z * cone0.z));
           if (c == 1u && d > cone0.w) a.w = __float_as_int(occ_val);
@@ -213,7 +255,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
     } else {
       for (int i = tid; i < np; i += VIS_THREADS) {
         const int64_t j = tile + i;
-        s_p0[i] = p.pix0[j];
+        int4 a = p.pix0[j];
+        if (bright) a.w = __float_as_int(bright[j]);
+        s_p0[i] = a;
         if (FRAC) s_p1[i] = p.pix1[j];
         if (COMP) s_lo[i] = p.plo[j];
         if (REF) s_qr[i] = p.pqr[j];
@@ -227,7 +271,13 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
           if (wv.x <= wv.y && wv.z + 1 < wv.w) {
             const int64_t lo_idx = (int64_t)wv.x * p.res + wv.z + 1;
             const int64_t hi_idx = (int64_t)wv.y * p.res + wv.w - 1;
-            if (lo_idx < tile + np && hi_idx >= tile) hit = true;
+            int64_t tlo = tile, thi = tile + np - 1;  // fine indices the tile's pixels cover
+            if (p.use_map) {
+              const int2 tr = p.map.tile_rng[tile / VIS_P];
+              tlo = tr.x;
+              thi = tr.y;
+            }
+            if (lo_idx <= thi && hi_idx >= tlo) hit = true;
           }
         }
       }
@@ -257,9 +307,13 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         if (COMP) lo = s_lo[pi];
         const int2 qr = s_qr[pi];
         const float c0 = __int_as_float(a.w);
+        int4 bx = make_int4(0, 0, 0, 0);
+        if (p.use_map) bx = __ldg(p.map.box + tile + pi);
 #pragma unroll
         for (int i = 0; i < VIS_TK; ++i) {
-          const float c = ref_hit(sm.win[tid + i * VIS_THREADS], qr.x, qr.y, tile + pi, p.res) ? occ_val : c0;
+          const int4 wv = sm.win[tid + i * VIS_THREADS];
+          const float c = p.use_map ? ref_map_value(p.map, wv, bx, c0, occ_val, tile + pi, p.res)
+                                    : (ref_hit(wv, qr.x, qr.y, tile + pi, p.res) ? occ_val : c0);
           vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
                                tr[i], ti[i]);
         }
@@ -270,7 +324,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 #pragma unroll
       for (int i = 0; i < VIS_TK; ++i) {
         const int64_t k = row0 + tid + i * VIS_THREADS;
-        const int pk = __ldg(&p.rows0[k].w);
+        const int pk = __ldg(p.rowsat + k);
         gm[i] = sat_gm(pk);
         gn[i] = sat_gn(pk);
       }
@@ -306,36 +360,65 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   // V = -ar + i ai  (the angle carried an extra half turn)
 #pragma unroll
   for (int i = 0; i < VIS_TK; ++i) {
-    const int64_t k = row0 + tid + i * VIS_THREADS;
+    const int64_t kl = local0 + tid + i * VIS_THREADS;
     const float4 t = sm.acc[tid + i * VIS_THREADS];
     const float ar = t.x, ai = t.y;
-    if (k < p.K) {
+    if (kl < nvalid) {
+      const int64_t k = row_first + kl;
       if (p.nsplit == 1) p.out[k] = make_float2(-ar, ai);
       else p.out[(int64_t)split * p.K + k] = make_float2(ar, ai);
     }
   }
 }
 
+// Integer-valued uvw (the reference's ceil(), MIncline:156-158) need no
+// fractional term; the row prep sets flags[0] when any uvw is fractional and
+// the kernel picks its loop from that flag (uniform branch, no host sync).
+//
+// Persistent: grid = resident CTAs; each CTA takes the next work item (rowblock,
+// pixel chunk) from an atomic counter until none are left, so uneven items
+// (channels, occluded fractions) balance without a wave tail.  The counter is
+// reset by the host before the launch; no CTA ever waits on another.
 template <int MASK, bool COMP>
 __global__ void __launch_bounds__(VIS_THREADS, VISS_VIS_MINB) vis_fast_kernel(const VisParams p) {
   __shared__ VisSmem<MASK, COMP> sm;
-  if (__ldg(p.flags) != 0) vis_body<MASK, true, COMP>(p, sm);
-  else vis_body<MASK, false, COMP>(p, sm);
+  __shared__ int s_item;
+  const bool frac = __ldg(p.flags + FLAG_FRAC) != 0;
+  for (;;) {
+    __syncthreads();  // everyone has read the previous item
+    if (threadIdx.x == 0) s_item = atomicAdd(p.flags + FLAG_VIS_COUNTER, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= p.nitems) break;
+    const int64_t rb = item / p.nsplit;
+    const int split = item - (int)(rb * p.nsplit);
+    int ch = 0;
+    while (ch + 1 < p.ch.nch && rb >= p.ch.rb_off[ch + 1]) ++ch;
+    const int64_t nvalid = p.ch.row_off[ch + 1] - p.ch.row_off[ch];
+    if (frac) vis_body<MASK, true, COMP>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
+    else vis_body<MASK, false, COMP>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
+  }
 }
 
+// Persistent grid: resident CTAs of this kernel (capped by ctas_per_sm) on every SM.
 template <int MASK>
-static void launch_mask(const VisParams& p, dim3 grid, bool comp, cudaStream_t st) {
-  if (comp) vis_fast_kernel<MASK, true><<<grid, VIS_THREADS, 0, st>>>(p);
-  else vis_fast_kernel<MASK, false><<<grid, VIS_THREADS, 0, st>>>(p);
+static void launch_mask(const VisParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
+  if (comp) {
+    const int g = persistent_grid(vis_fast_kernel<MASK, true>, VIS_THREADS, ctas_per_sm, p.nitems);
+    vis_fast_kernel<MASK, true><<<g, VIS_THREADS, 0, st>>>(p);
+  } else {
+    const int g = persistent_grid(vis_fast_kernel<MASK, false>, VIS_THREADS, ctas_per_sm, p.nitems);
+    vis_fast_kernel<MASK, false><<<g, VIS_THREADS, 0, st>>>(p);
+  }
 }
 
-int launch_vis_fast(const VisParams& p, int64_t nrb, bool comp, cudaStream_t st) {
-  const dim3 grid((unsigned)nrb, (unsigned)p.nsplit);
+int launch_vis_fast(const VisParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
+  if (p.nitems <= 0) return VISS_OK;
   switch (p.mask) {
-    case VISS_MASK_NONE: launch_mask<VISS_MASK_NONE>(p, grid, comp, st); break;
-    case VISS_MASK_REF_QUIRK: launch_mask<VISS_MASK_REF_QUIRK>(p, grid, comp, st); break;
-    case VISS_MASK_REF_INTENDED: launch_mask<VISS_MASK_REF_INTENDED>(p, grid, comp, st); break;
-    case VISS_MASK_GEOMETRIC: launch_mask<VISS_MASK_GEOMETRIC>(p, grid, comp, st); break;
+    case VISS_MASK_NONE: launch_mask<VISS_MASK_NONE>(p, ctas_per_sm, comp, st); break;
+    case VISS_MASK_REF_QUIRK: launch_mask<VISS_MASK_REF_QUIRK>(p, ctas_per_sm, comp, st); break;
+    case VISS_MASK_REF_INTENDED: launch_mask<VISS_MASK_REF_INTENDED>(p, ctas_per_sm, comp, st); break;
+    case VISS_MASK_GEOMETRIC: launch_mask<VISS_MASK_GEOMETRIC>(p, ctas_per_sm, comp, st); break;
     default: return fail(VISS_ERR_INVALID, "unknown mask mode");
   }
   VISS_LAUNCH_CHECK("vis_fast_kernel");
@@ -384,6 +467,12 @@ struct PlainVisArgs {
   float trail;  // 1 + n_offset
   double R;
   float2* out;
+  // non-identity fine->coarse map: FF, NXq (float or int), countLoc
+  const float* FF;
+  const float* NXq_f;
+  const int32_t* NXq_i;
+  const int32_t* countLoc;
+  int64_t X;
 };
 
 __global__ void vis_plain_kernel(const PlainVisArgs a) {
@@ -407,10 +496,36 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
   }
   const float m2pi = -2.0f * (float)kPi;
   float ar = 0.f, ai = 0.f;
+  int64_t start = 0;
   for (int64_t j = 0; j < a.J; ++j) {
-    float c = a.bright[j];
-    if (a.trunc) c = (float)(int)c;
-    if (wv.x <= wv.y) {
+    float c;
+    if (a.countLoc) {
+      // vissGen10M_shade.cu:123-135: C = mean over the pixel's fine members of FF, 240 inside the window
+      const int cnt = a.countLoc[j];
+      float sum = 0.f;
+      for (int e = 0; e < cnt; ++e) {
+        const int64_t loc = a.NXq_f ? (int64_t)a.NXq_f[start + e] : (int64_t)a.NXq_i[start + e];
+        if (loc < 0 || loc >= a.X || start + e >= a.X) {  // outside the fine grid: no read, NaN
+          sum = nanf("");
+          continue;
+        }
+        float ff = a.FF[loc];
+        if (a.trunc) ff = (float)(int)ff;
+        if (wv.x <= wv.y && ref_hit_general(wv, loc, a.res)) ff = a.occ;
+        sum += ff;
+      }
+      start += cnt;
+      c = sum / (float)cnt;
+    } else {
+      c = a.bright[j];
+      if (a.trunc) c = (float)(int)c;
+    }
+    if (a.countLoc) {
+      if (geo) {
+        const float sx = a.l[j], sy = a.m[j], sz = a.n[j];
+        if (geo_test_plain(sx, sy, sz, d1, p1, a.R) || geo_test_plain(sx, sy, sz, d2, p2, a.R)) c = a.occ;
+      }
+    } else if (wv.x <= wv.y) {
       const int64_t q = j / a.res, r = j % a.res;
       if (ref_hit(wv, (int)q, (int)r, j, a.res)) c = a.occ;
     } else if (geo) {
@@ -429,8 +544,12 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
 }
 
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st) {
+                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
+                     const viss_fine_map* map) {
   PlainVisArgs a{};
+  if (map) {
+    a.FF = map->FF; a.NXq_f = map->NXq_f; a.NXq_i = map->NXq_i; a.countLoc = map->countLoc; a.X = map->X;
+  }
   a.satdir = satdir;
   a.u = vis.u; a.v = vis.v; a.w = vis.w;
   a.l = sky.l; a.m = sky.m; a.n = sky.n; a.bright = sky.bright;

@@ -78,6 +78,11 @@ constexpr int REC_Q = 256;                // visibilities per shared-memory tile
 #define VISS_REC_MINB 3
 #endif
 
+// Channels of one batched pass, and visibility segments of its reconstruction
+// (their tables travel in the kernel parameters).
+constexpr int VISS_MAX_CH = VISS_MAX_CHANNELS;
+constexpr int VISS_MAX_SEG = 96;
+
 // Geometric test: |e| below this margin is re-decided in double.
 constexpr float GEO_EPS = 2e-6f;
 
@@ -89,11 +94,11 @@ enum PixClass : int { CLS_VIS = 0, CLS_OCC = 1, CLS_MIX = 2 };
 //   A' = round(x * 2^30)           -- for the fractional part of u (|x| < 2)
 //   lo = x - A*2^-32 (float)       -- compensation of the rounding of A
 // A visibility coordinate u is split u = U + f, U = floor(u + 1/2), f in [-1/2, 1/2).
-// Phase (turns * 2^32, mod 2^32) = U*A + V*B + W*C + bias_k + frac, where the
-// fractional part delta = f_u*x + f_v*y + f_w*z' (FP32, |delta| < 2, z' = s*n) is
-// folded in with one FADD: the bits of (delta + 6.0f) hold delta in units of
-// 2^-21 turns above the constant 0x40C00000, whose shift by 11 vanishes mod 2^32,
-// so frac = bits(delta + 6) << 11.  bias_k carries f_w*s*n_offset.
+// Phase (turns * 2^32, mod 2^32) = U*A + V*B + W*C + bias_k; bias_k carries
+// PHASE_BIAS, f_w*s*n_offset and (reconstruction) the phase of the row's
+// visibility.  The fractional part delta = f_u*x + f_v*y + f_w*z' (FP32, z' = s*n,
+// |delta| <= 0.87 turn) and the compensation terms are added to the FP32 angle
+// with one FFMA after the fixed-point turn has been converted.
 __device__ __forceinline__ uint32_t fix32(double x) {
   return (uint32_t)(unsigned long long)llrint(x * 4294967296.0);
 }
@@ -105,13 +110,10 @@ __device__ __forceinline__ float turns_to_angle(uint32_t q) {
   return fmaf(f, K2PI, KM3PI);
 }
 
-// delta (turns, |delta| < 2) -> its fixed-point phase contribution (units 2^-32, resolution 2^-21)
-__device__ __forceinline__ uint32_t frac_phase(float delta) {
-  return __float_as_uint(delta + 6.0f) << 11;
-}
-
 // Satellite indices of a visibility (geometric mask): gm = snapshot*nsat + m in the
-// low 26 bits, n - m + 32 in the top 6.
+// low 26 bits, n - m + 32 in the top 6.  Padding rows carry PAD_PACKED (both
+// indices 0, always in range).
+constexpr int PAD_PACKED = 32 << 26;
 __device__ __forceinline__ int sat_gm(int packed) { return packed & 0x3ffffff; }
 __device__ __forceinline__ int sat_gn(int packed) { return (packed & 0x3ffffff) + (int)((uint32_t)packed >> 26) - 32; }
 
@@ -154,13 +156,30 @@ struct PixPrepArgs {
   int2* qr;       // {j / res, j % res}
 };
 
+// Visibility rows of a (batched) pass: channel c owns input rows
+// [row_off[c], row_off[c+1]).  The vis pass pads every channel to whole blocks
+// of VIS_ROWS rows: its padded blocks are [rb_off[c], rb_off[c+1]).
+struct ChannelRows {
+  int nch;
+  int64_t rb_off[VISS_MAX_CH + 1];
+  int64_t row_off[VISS_MAX_CH + 1];
+};
+
+// Row records (both passes):
+//   rows0 {U, V, W, bias}            integer uvw and the fixed-point phase bias
+//   rows1 {f_u, f_v, f_w, c}         fractional uvw; c = |wgt V| (recon) or 0 (vis)
+//   rowsat packed satellite indices  (geometric mask)
+//   rowsf {U, V, W as float, 0}      (compensation)
+//   win                              vis REF: {lo_a, lo_b, M1, M2}; recon REF: {tmax, pmax, 0, 0}
 struct RowPrepArgs {
   double sn, n_offset;   // z = sn * (n + n_offset): the f_w * sn * n_offset part goes to the row bias
+  ChannelRows ch;        // padded (vis): row pr of block b of channel c is input row
+  bool padded;           //   row_off[c] + pr - rb_off[c]*VIS_ROWS when below row_off[c+1]
   const float* u;
   const float* v;
   const float* w;
   const float* wgt;
-  const float* V;        // recon: K x 2
+  const float* V;        // recon: K x 2, folded into bias and c
   const int32_t* shade;  // K x 4
   const int32_t* snap;
   const int32_t* pair;
@@ -169,12 +188,27 @@ struct RowPrepArgs {
   int64_t K, Kpad;
   int mask_mode;
   int recon_mask;
-  int4* rec0;   // {U, V, W, packed satellite indices}
-  int4* rec1;   // {f_u, f_v, f_w (float bits), phase bias}
-  float4* uf;   // {U, V, W as float, 0}   (compensation)
-  int4* win;    // vis REF: {lo_a, lo_b, M1, M2}; recon REF: {tmax, pmax, 0, 0}
-  float2* y;    // recon: wgt * V
-  int* flags;   // [0] |= any fractional uvw, [1] |= |U| out of range
+  int4* rows0;
+  float4* rows1;
+  int* rowsat;
+  float4* uf;
+  int4* win;
+  int* flags;   // [0] |= any fractional uvw, [1] |= |U| out of range, |= 2 bad satellite index
+};
+
+// flags words of a pass
+constexpr int FLAG_FRAC = 0, FLAG_ERR = 1, FLAG_VIS_COUNTER = 8, FLAG_REC_COUNTER = 9, FLAG_WORDS = 64;
+
+// A fine sky grid mapped onto the coarse pixels: pixel (position) j has
+// members[start_j .. start_j + cnt_j), fine indices as the reference reads them
+// (NXq[c] truncated to an integer).
+struct FineMapDev {
+  const int4* box;        // [Jpad] {qmin, qmax, rmin, rmax}: rows/columns (i / res, i % res) of the members
+  const int2* mem;        // [Jpad] {start, cnt}
+  const int* members;     // [X]
+  const float* FF;        // [X] fine brightness
+  const int2* tile_rng;   // [Jpad / VIS_P] {min, max} member fine index of each pixel tile
+  int trunc;              // int truncation of FF (the plain reference variant)
 };
 
 struct VisParams {
@@ -184,7 +218,8 @@ struct VisParams {
   const float4* pgeo;
   const int2* pqr;
   const int4* rows0;
-  const int4* rows1;
+  const float4* rows1;
+  const int* rowsat;
   const float4* rowsf;
   const int4* win;
   const float4* satdir;   // [S*nsat] {p_hat, cos_alpha}
@@ -193,15 +228,23 @@ struct VisParams {
   const float* m;
   const float* n;
   const float* sat_pos;
-  const int* flags;
-  float2* out;            // partial [nsplit][K] or final [K]
+  const float* bright;    // [nch][J] per-channel brightness, or NULL (pixel records carry it)
+  int* flags;             // flags[FLAG_VIS_COUNTER]: next work item
+  float2* out;            // partial [nsplit][K] or final [K] (K = all channels' visibilities)
   int64_t K, J;
   int64_t jchunk;
   int nsplit;
+  int nitems;             // work items (rowblock, pixel chunk) = nrb * nsplit
   int res;
   float occ_val;
   double R;
   int mask;               // VISS_MASK_*
+  ChannelRows ch;
+  // non-identity fine->coarse map (REF masks): a pixel's brightness for row k is
+  // the mean over its fine members, each replaced by the occluded value inside
+  // k's window (vissGen10M_shade.cu:120-136)
+  FineMapDev map;
+  int use_map;            // 0: identity map
 };
 
 struct ReconParams {
@@ -211,27 +254,44 @@ struct ReconParams {
   const float4* pgeo;
   const int2* pqr;
   const int4* rows0;
-  const int4* rows1;
+  const float4* rows1;
+  const int* rowsat;
   const float4* rowsf;
   const int4* win;
-  const float2* y;
   const float4* satdir;
   const float4* scones;   // [S*2] per-snapshot cones
   const float* l;
   const float* m;
   const float* n;
   const float* sat_pos;
-  const int* flags;
+  int* flags;             // flags[FLAG_REC_COUNTER]: next work item
   const int32_t* perm;    // position -> pixel (NULL: identity)
-  float2* out;            // partial [nsplit][J] by position, or final F by pixel
+  float2* out;            // F [nch][J] by pixel
+  float2* partial;        // [nslot][J] by position (segments that share a channel)
   int64_t K, J;
-  int64_t kchunk;
-  int nsplit;
   int res;
   int nsat;
   double R;
-  float norm;
   int recon_mask;
+  // work items (segment, pixel block): segments are row ranges of one channel,
+  // longest first; item i is segment i / npb, pixel block i % npb
+  int nitems;
+  int npb;
+  int nseg;
+  int64_t seg_lo[VISS_MAX_SEG], seg_hi[VISS_MAX_SEG];
+  int seg_ch[VISS_MAX_SEG], seg_slot[VISS_MAX_SEG];   // slot -1: the segment writes F directly
+  float ch_norm[VISS_MAX_CH];
+};
+
+// Per-channel sum of partial slots (channels split into several segments).
+struct RecReduceParams {
+  const float2* partial;
+  const int32_t* perm;
+  float2* out;            // F [nch][J]
+  int64_t J;
+  int nch;
+  int slot0[VISS_MAX_CH], nslot[VISS_MAX_CH];
+  float norm[VISS_MAX_CH];
 };
 
 // ------------------------------------------------------------- launchers
@@ -245,18 +305,25 @@ int pixel_order(const float* l, const float* m, const float* n, int64_t J, void*
                 int32_t* perm, cudaStream_t st);
 int launch_prep_rows(const RowPrepArgs& a, bool recon, cudaStream_t st);
 int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satdir, cudaStream_t st);
-int launch_prep_rowblock_cones(const int4* rows0, const int4* rows1, const float4* satdir, int64_t K,
-                               int rows_per_block, int64_t nblocks, float4* cones, cudaStream_t st);
+int launch_prep_rowblock_cones(const int* rowsat, const float4* satdir, const ChannelRows& ch, int64_t nblocks,
+                               float4* cones, cudaStream_t st);
 int launch_prep_snapshot_cones(const float4* satdir, int64_t S, int nsat, float4* cones, cudaStream_t st);
 
-int launch_vis_fast(const VisParams& p, int64_t nrb, bool compensated, cudaStream_t st);
+// Persistent launches: ctas_per_sm 0 = as many as fit.
+int launch_vis_fast(const VisParams& p, int ctas_per_sm, bool compensated, cudaStream_t st);
+// Fine->coarse map records for the vis pass: per-pixel base brightness (mean of
+// FF over the members), member boxes and ranges, per-tile fine-index ranges.
+size_t fine_map_scratch(int64_t J);
+int prep_fine_map(const float* NXq_f, const int32_t* NXq_i, const int32_t* countLoc, const float* FF, int64_t J,
+                  int64_t X, int res, int trunc, int64_t Jpad, float* base, int4* box, int2* mem, int* members,
+                  int2* tile_rng, void* scratch, size_t scratch_bytes, int* flags, cudaStream_t st);
 int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st);
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
-                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st);
+                     const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
+                     const viss_fine_map* map = nullptr);
 
-int launch_recon_fast(const ReconParams& p, int64_t npb, bool compensated, cudaStream_t st);
-int launch_recon_reduce(const float2* partial, int nsplit, int64_t J, float norm, const int32_t* perm, float2* out,
-                        cudaStream_t st);
+int launch_recon_fast(const ReconParams& p, int ctas_per_sm, bool compensated, cudaStream_t st);
+int launch_recon_reduce(const RecReduceParams& p, cudaStream_t st);
 int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                        const viss_geometry* geo, const float* V, const float* ratios, const float4* satdir,
                        const float* dlmn, float2* out, cudaStream_t st);
@@ -273,5 +340,16 @@ __device__ __forceinline__ bool geo_test_plain(float sx, float sy, float sz, con
 }
 
 int device_sm_count();
+
+// Grid of a persistent kernel: its resident CTAs per SM (capped by
+// ctas_per_sm when > 0) on every SM, no more than the work items.
+template <class Kernel>
+inline int persistent_grid(Kernel k, int threads, int ctas_per_sm, int nitems) {
+  int occ = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, 0) != cudaSuccess || occ < 1) occ = 1;
+  if (ctas_per_sm > 0 && ctas_per_sm < occ) occ = ctas_per_sm;
+  const int64_t g = (int64_t)occ * device_sm_count();
+  return (int)(g < nitems ? g : nitems);
+}
 
 }  // namespace viss

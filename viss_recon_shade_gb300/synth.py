@@ -124,3 +124,69 @@ def make_uvw(wl: Workload, device="cuda"):
         pos, pos64 = orbit_positions(cfg, device=device, want_f64=True)
         u, v, w, snap, pair = baseline_uvw(pos, wl.lambda_m, ordered=wl.ordered, rounding=False, pos64=pos64)
     return dict(u=u, v=v, w=w, snap=snap, pair=pair, sat_pos=pos)
+
+
+@dataclass(frozen=True)
+class BatchWorkload:
+    """Many frequency channels in one pass: nch channels log-spaced over
+    [fmin, fmax], each with its own snapshot count (uniform in [smin, smax],
+    multiples of 16, at least 128, seeded) and orbit phase (the period index, which moves the
+    orbit's node and window start), and a power-law brightness per channel."""
+    name: str = "batch64"
+    nch: int = 64
+    fmin_hz: float = 1e6
+    fmax_hz: float = 30e6
+    smin: int = 4096
+    smax: int = 65536
+    J: int = 49152
+    nsat: int = 8
+    n_points: int = 500
+    seed: int = 0
+    a_km: float = MOON_R + 300.0
+    incl_deg: float = 30.0
+
+    def freqs(self) -> np.ndarray:
+        return np.geomspace(self.fmin_hz, self.fmax_hz, self.nch)
+
+    def snapshots(self) -> np.ndarray:
+        rng = np.random.default_rng(self.seed)
+        return rng.integers(self.smin // 16, self.smax // 16 + 1, self.nch) * 16
+
+    @property
+    def npairs(self) -> int:
+        return self.nsat * (self.nsat - 1) // 2
+
+
+BATCH_WORKLOADS = {
+    "batch64": BatchWorkload(),
+    "batch5_small": BatchWorkload(name="batch5_small", nch=5, smin=128, smax=512, J=12288, n_points=20),
+}
+
+
+def make_batch(bw: BatchWorkload, device="cuda"):
+    """Rows of every channel back to back (uvw, snap into one satellite-position
+    array, pair), row offsets, per-channel brightness [nch, J] and the sky."""
+    import torch
+
+    from .api import OrbitConfig, baseline_uvw, orbit_positions
+    l, m, n = fibonacci_sphere(bw.J)
+    r1, r2 = log_separations(bw.nsat)
+    us, vs, ws, snaps, pairs, poss = [], [], [], [], [], []
+    row_off = [0]
+    s_off = 0
+    bright = np.empty((bw.nch, bw.J), dtype=np.float32)
+    for c, (f, S) in enumerate(zip(bw.freqs(), bw.snapshots())):
+        counts = 16 if 3 * int(S) // 16 >= 360 else 1  # the orbit kernel wants >= 360 samples per orbit
+        cfg = OrbitConfig(nsat=bw.nsat, orbit_res=3 * int(S) // counts, orbit_counts=counts, index=1 + c,
+                          a_km=bw.a_km, incl_deg=bw.incl_deg, r1_m=r1, r2_m=r2, fp64=True)
+        pos, pos64 = orbit_positions(cfg, device=device, want_f64=True)
+        u, v, w, snap, pair = baseline_uvw(pos, 3e8 / f, ordered=False, rounding=False, pos64=pos64)
+        us.append(u); vs.append(v); ws.append(w); pairs.append(pair); poss.append(pos)
+        snaps.append(snap + s_off)
+        s_off += pos.shape[0]
+        row_off.append(row_off[-1] + u.numel())
+        bright[c] = powerlaw_sky(n, f / 1e6, seed=bw.seed, n_points=bw.n_points)
+    cat = torch.cat
+    return dict(u=cat(us), v=cat(vs), w=cat(ws), snap=cat(snaps), pair=cat(pairs), sat_pos=cat(poss),
+                row_off=np.asarray(row_off, dtype=np.int64), bright=torch.from_numpy(bright).to(device),
+                l=l, m=m, n=n, freqs=bw.freqs())
