@@ -34,6 +34,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Gterms/s shaded vis-DFT + recon, 1 GB300, chosen vs plain at ≤1e-5 rel err"
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
+# capture of this workload at full size; profiles/dram_traffic_cfg2_10MHz.md has the command.
+TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 110.97e6, "recon_fast_kernel": 123.49e6}}
 UNIT = "Gterms/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -75,11 +78,13 @@ def barrier(ws):
 
 
 def max_over_ranks(x: float, ws: int) -> float:
+    """The slowest rank's time (replicas: each rank runs the whole workload on its GPU)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -260,7 +265,8 @@ def run_ours(args, ws, rank, local):
                 "unit": "G SFU op/s", "frac": round(achieved / sfu_peak, 4),
                 "peak_source": "measured: viss_sfu_probe (8 independent __sincosf chains per thread) in this run",
                 "algorithmic_per_term": "2 SFU ops (sin, cos) + 6 FMA-pipe ops (vis) / 8 (recon)",
-                "traffic": None, "sm_count": props.multi_processor_count,
+                "traffic": TRAFFIC_BYTES.get(wl.name, {}).get(dom), "traffic_unit": "bytes per launch (ncu)",
+                "sm_count": props.multi_processor_count,
                 "vis_ms": round(vis_ms, 3), "recon_ms": round(rec_ms, 3)}
 
     # ---- plain (the reference's FP32 method restated) -------------------------
