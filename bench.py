@@ -35,7 +35,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "Gterms/s shaded vis-DFT + recon, 1 GB300, chosen vs plain at ≤1e-5 rel err"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
-# capture of this workload at full size; profiles/dram_traffic_cfg2_10MHz.md has the command.
+# capture of this workload at full size (the command is kept with the ncu summaries).
 TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 110.97e6, "recon_fast_kernel": 123.49e6}}
 UNIT = "Gterms/s"
 L2_FLUSH_BYTES = 256 << 20
@@ -174,7 +174,7 @@ def run_ours(args, ws, rank, local):
     wl, d = load_workload(args.workload)
     K, J = d["u"].numel(), d["l"].numel()
     prec = choose_precision(d, args.precision)
-    cfg = V.DftConfig.north_star(precision=prec, occluded_value=0.0)
+    cfg = V.DftConfig.geometric(precision=prec, occluded_value=0.0)
     geo = dict(snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     Vout = torch.empty(K, dtype=torch.complex64, device="cuda")
@@ -474,7 +474,7 @@ def run_batch(args, ws, rank, local):
     t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
     lg, mg, ng = t(d["l"]), t(d["m"]), t(d["n"])
     prec = choose_precision(d, args.precision)
-    cfg = V.DftConfig.north_star(precision=prec, occluded_value=0.0)
+    cfg = V.DftConfig.geometric(precision=prec, occluded_value=0.0)
     ro = d["row_off"]
     K, J, nch = int(ro[-1]), bw.J, bw.nch
 

@@ -83,7 +83,7 @@ enum {                         /* phase + sincos arithmetic */
  * recon: F_j = norm * sum_k [not masked] wgt_k V_k exp(+2 pi i t_kj)
  * The reference uses phase_scale = 1/d with d = 2*RES/(RES-1) in integer arithmetic (= 2),
  * n_offset = 0 (its w(n-1) term and trailing e^{-2 pi i w/d} combine to w n), occluded_value 240,
- * norm = 1/K.  The spec convention is phase_scale = 1, n_offset = -1, occluded_value 0. */
+ * norm = 1/K.  The geometric-mask convention is phase_scale = 1, n_offset = -1, occluded_value 0. */
 typedef struct viss_dft_cfg {
   int32_t mask_mode;         /* VISS_MASK_* (vis) */
   int32_t recon_mask;        /* VISS_RECON_MASK_* (recon) */
@@ -187,6 +187,15 @@ VISS_API int viss_vis_dft_map(const viss_dft_cfg* cfg, const viss_sky* sky, cons
 VISS_API size_t viss_nxq_workspace(int64_t X, int64_t J);
 VISS_API int viss_nxq(const float* NX, int64_t X, int64_t J, int32_t* countLoc, int32_t* NXq, void* workspace,
                       size_t workspace_bytes, void* stream);
+
+/* Input problems a pass records instead of reading out of bounds (a pass never
+ * synchronises to look): after the pass has completed, reads the flag word at
+ * the start of its workspace (synchronises `stream`).  Bits: 1 = |uvw| >= 2^30,
+ * 2 = a snapshot or satellite index outside the geometry (that visibility's
+ * occlusion test used satellite 0 of snapshot 0), 4 = recon ratio arrays not of
+ * the reference's form, 8 = a fine-map index outside [0, X) (that pixel is NaN).
+ * No counterpart in the reference, which reads such inputs unchecked. */
+VISS_API int viss_workspace_flags(const void* workspace, int32_t* flags, void* stream);
 
 /* Batched passes: many frequency channels (or periods) in one persistent
  * launch.  The reference runs one channel per program run or per OpenMP

@@ -19,7 +19,7 @@ def setup():
     l, m, n, b = make_sky(wl)
     t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
     d.update(l=t(l), m=t(m), n=t(n), truth=t(b / b.max()))
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=0.0)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST, occluded_value=0.0)
     return V, wl, d, cfg
 
 

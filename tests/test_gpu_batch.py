@@ -37,7 +37,7 @@ def channel(d, c, V=None):
 def test_batch_matches_channels_run_alone(data, prec, mask):
     V, d = data
     p = {"fast": V.PREC_FAST, "comp": V.PREC_COMPENSATED, "plain": V.PREC_PLAIN}[prec]
-    cfg = V.DftConfig.north_star(precision=p)
+    cfg = V.DftConfig.geometric(precision=p)
     if mask == "none":
         cfg = cfg.with_(mask=V.MASK_NONE, recon_mask=V.RECON_MASK_NONE)
     b = V.ChannelBatch(cfg, d["u"], d["v"], d["w"], d["row_off"], d["lg"], d["mg"], d["ng"], d["bright"],
@@ -59,7 +59,7 @@ def test_batch_matches_channels_run_alone(data, prec, mask):
 
 def test_batch_channel_against_fp64_oracle(data, oracle):
     V, d = data
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST)
     b = V.ChannelBatch(cfg, d["u"], d["v"], d["w"], d["row_off"], d["lg"], d["mg"], d["ng"], d["bright"],
                        snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
     Vb = b.vis()
@@ -84,7 +84,7 @@ def test_batch_channel_against_fp64_oracle(data, oracle):
 
 def test_graph_replay_and_tunings_agree(data):
     V, d = data
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST)
     b = V.ChannelBatch(cfg, d["u"], d["v"], d["w"], d["row_off"], d["lg"], d["mg"], d["ng"], d["bright"],
                        snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
     b.step()

@@ -240,7 +240,7 @@ def test_vis_recon_geometric(V, oracle, occ, prec):
     J = 3000
     l, m, n, b = sky(J)
     p = {"fast": V.PREC_FAST, "comp": V.PREC_COMPENSATED, "plain": V.PREC_PLAIN}[prec]
-    cfg = V.DftConfig.north_star(precision=p, occluded_value=occ)
+    cfg = V.DftConfig.geometric(precision=p, occluded_value=occ)
     Vg = V.vis_dft(cfg, u, v, w, *map(cu, (l, m, n, b)), snap=snap, pair=pair, sat_pos=pos).cpu().numpy()
     hn = lambda t: t.cpu().numpy()  # noqa: E731
     geo = oracle.make_geo(hn(pos), hn(snap), hn(pair))
@@ -267,7 +267,7 @@ def test_geometric_mask_exact_counts(V, oracle):
     J = 4000
     l, m, n, _ = sky(J)
     z = torch.zeros(K, dtype=torch.float32, device="cuda")
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=1.0)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST, occluded_value=1.0)
     Vg = V.vis_dft(cfg, z, z, z, *map(cu, (l, m, n)), cu(np.zeros(J, np.float32)), snap=snap, pair=pair,
                    sat_pos=pos).cpu().numpy()
     hn = lambda t: t.cpu().numpy()  # noqa: E731
@@ -296,7 +296,7 @@ def test_linearity_and_adjoint_large(V):
     d = make_uvw(wl)
     l, m, n, b = make_sky(wl)
     J = l.size
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=0.0)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST, occluded_value=0.0)
     rng = np.random.default_rng(11)
     x1 = rng.uniform(0, 1, J).astype(np.float32)
     x2 = rng.uniform(0, 1, J).astype(np.float32)

@@ -47,6 +47,15 @@ def synth_uvw_shade(K, res, seed=1):
     return u, v, w, raw
 
 
+def read_sidecar(path):
+    """The drop-in programs' binary sidecar: 'VISS', version, type (1 = complex64), reserved, int64 count."""
+    raw = Path(path).read_bytes()
+    hdr = np.frombuffer(raw[:16], np.uint32)
+    assert hdr[0] == 0x53534956 and hdr[1] == 1 and hdr[2] == 1
+    n = int(np.frombuffer(raw[16:24], np.int64)[0])
+    return np.frombuffer(raw[24:], np.complex64, count=n)
+
+
 def run(args, cwd):
     r = subprocess.run([str(a) for a in args], cwd=cwd, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -64,9 +73,13 @@ def test_vissGen10M_shade_dropin(oracle, tmp_path):
     fd.mkdir()
     np.savetxt(fd / "updated_uvw1frequency10M.txt", np.stack([u, v, w, freq], -1), fmt="%g")
     np.savetxt(fd / "shadeM1frequency10M.txt", raw, fmt="%d")
-    out = run([BIN / "vissGen10M_shade", "--res", res], tmp_path)
+    out = run([BIN / "vissGen10M_shade", "--res", res, "--sidecar"], tmp_path)
     assert "Compute Viss Cost Time" in out
     F = read_col(tmp_path / "F_recon_10M" / "F1period10M.txt")
+    Fs = read_sidecar(tmp_path / "F_recon_10M" / "F1period10M.F.c64")
+    Vs = read_sidecar(tmp_path / "F_recon_10M" / "F1period10M.V.c64")
+    assert Fs.shape == (J,) and Vs.shape == (K,)
+    assert np.abs(F - Fs.real).max() <= 1e-5 * np.abs(Fs.real).max()  # the text keeps 6 digits
     M = oracle.normalise_shade(raw)
     ncl = np.clip(n, -1, 1)
     V = oracle.vis_dft(oracle.make_cfg(mask_mode=1, res=res, trunc=True, occluded_value=240.0), u, v, w, l, m, ncl, FF,
@@ -75,6 +88,7 @@ def test_vissGen10M_shade_dropin(oracle, tmp_path):
                       V.astype(np.complex64), l, m, ncl, shade=M)
     assert F.shape == (J,)
     assert np.abs(F - Fo.real).max() / np.abs(Fo.real).max() < 2e-5
+    assert np.abs(Fs - Fo).max() / np.abs(Fo).max() < 2e-5
     # optim2 naming and period loop (days/start-period flags as in its main)
     run([BIN / "vissGen10M_shade_optim2", "--res", res, "--start-period", 0, "--days", 1], tmp_path)
     assert (tmp_path / "F_recon_10M" / "F1period10M_optim2.txt").exists()

@@ -109,7 +109,7 @@ def test_bench_workload_accuracy(V, oracle):
     wl = WORKLOADS["cfg2_10MHz"]
     d = make_uvw(wl)
     l, m, n, b = make_sky(wl)
-    cfg = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=0.0)
+    cfg = V.DftConfig.geometric(precision=V.PREC_FAST, occluded_value=0.0)
     args = dict(snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
     Vg = V.vis_dft(cfg, d["u"], d["v"], d["w"], cu(l), cu(m), cu(n), cu(b), **args)
     Fg = V.recon(cfg, d["u"], d["v"], d["w"], Vg, cu(l), cu(m), cu(n), **args)

@@ -34,11 +34,11 @@ def test_precision_sweep_30MHz(oracle):
     errs = {}
     Vref = None
     for name, prec in (("plain", V.PREC_PLAIN), ("fast", V.PREC_FAST), ("comp", V.PREC_COMPENSATED)):
-        cfg = V.DftConfig.north_star(precision=prec)
+        cfg = V.DftConfig.geometric(precision=prec)
         Vg = V.vis_dft(cfg, d["u"], d["v"], d["w"], cu(l), cu(m), cu(n), cu(b), **geo)
         if Vref is None:
             # recon errors are measured on the same input visibilities for every mode
-            Vref = V.vis_dft(V.DftConfig.north_star(precision=V.PREC_COMPENSATED), d["u"], d["v"], d["w"], cu(l),
+            Vref = V.vis_dft(V.DftConfig.geometric(precision=V.PREC_COMPENSATED), d["u"], d["v"], d["w"], cu(l),
                              cu(m), cu(n), cu(b), **geo)
             Fo = oracle.recon(oc, u, v, w, None, h(Vref), l[pix], m[pix], n[pix], geo=oracle.make_geo(pos, snap, pair))
         Fg = V.recon(cfg, d["u"], d["v"], d["w"], Vref, cu(l), cu(m), cu(n), **geo)

@@ -44,7 +44,7 @@ def test_noalloc_matches_workspace_entry_point_twice():
     import viss_recon_shade_gb300 as V
     from viss_recon_shade_gb300 import _lib as L
     stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
-    cfg_py = V.DftConfig.north_star(precision=V.PREC_FAST, occluded_value=0.0)
+    cfg_py = V.DftConfig.geometric(precision=V.PREC_FAST, occluded_value=0.0)
     for seed in (0, 1):  # two calls in a row on the shared scratch, different inputs
         d = _case(seed)
         cfg, sky, vis, geo = _structs(L, d, cfg_py)
@@ -69,7 +69,7 @@ def test_noalloc_rejects_passes_beyond_its_scratch():
     import viss_recon_shade_gb300 as V
     from viss_recon_shade_gb300 import _lib as L
     d = _case(0, orbit_counts=24)  # 28 x 49,152 visibilities: needs more than the built-in scratch
-    cfg, sky, vis, geo = _structs(L, d, V.DftConfig.north_star())
+    cfg, sky, vis, geo = _structs(L, d, V.DftConfig.geometric())
     assert L.lib.viss_vis_dft_workspace(C.byref(cfg), vis.K, sky.J, C.byref(geo)) > (32 << 20)
     out = torch.empty(vis.K, dtype=torch.complex64, device="cuda")
     rc = L.lib.viss_vis_dft_noalloc(C.byref(cfg), C.byref(sky), C.byref(vis), C.byref(geo),

@@ -51,7 +51,7 @@ class DftConfig:
                          phase_scale=1.0 / reference_d(res), n_offset=0.0)
 
     @staticmethod
-    def north_star(precision: int = PREC_FAST, occluded_value: float = 0.0) -> "DftConfig":
+    def geometric(precision: int = PREC_FAST, occluded_value: float = 0.0) -> "DftConfig":
         """V_k = sum_j I_j mask_kj exp(-2 pi i (u l + v m + w (n - 1))) with the geometric mask."""
         return DftConfig(mask=MASK_GEOMETRIC, recon_mask=RECON_MASK_GEOMETRIC, precision=precision, res=0,
                          occluded_value=occluded_value, phase_scale=1.0, n_offset=-1.0)

@@ -352,6 +352,7 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
     return VISS_OK;
   }
   p.layout(ws);
+  VISS_CUDA(cudaMemsetAsync(p.flags, 0, FLAG_WORDS * sizeof(int), st));
   if (p.plain) {
     // the reference's form: one launch per channel
     if (p.geo && (rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
@@ -366,7 +367,6 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
     }
     return VISS_OK;
   }
-  VISS_CUDA(cudaMemsetAsync(p.flags, 0, FLAG_WORDS * sizeof(int), st));
   if (map && (rc = prep_fine_map(map->NXq_f, map->NXq_i, map->countLoc, map->FF, sky.J, map->X, cfg.res,
                                  cfg.trunc_brightness, p.Jpad, p.mbase, p.mbox, p.mmem, p.members, p.mtile,
                                  p.mscratch, p.mscratch_bytes, p.flags, st)))
@@ -625,6 +625,16 @@ static int check_vis_call(const viss_dft_cfg* cfg, const viss_sky* sky, const vi
   if (own_bright && cfg->trunc_brightness && cfg->precision != VISS_PREC_PLAIN)
     return fail(VISS_ERR_UNSUPPORTED, "trunc_brightness with per-channel brightness");
   if (cfg->mask_mode == VISS_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
+  return VISS_OK;
+}
+
+int viss_workspace_flags(const void* workspace, int32_t* flags, void* stream) {
+  if (!workspace || !flags) return fail(VISS_ERR_INVALID, "workspace or flags is NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // the flag words are the first carve of every pass's workspace
+  VISS_CUDA(cudaMemcpyAsync(flags, static_cast<const int*>(workspace) + FLAG_ERR, sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, st));
+  VISS_CUDA(cudaStreamSynchronize(st));
   return VISS_OK;
 }
 

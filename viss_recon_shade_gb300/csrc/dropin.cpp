@@ -85,6 +85,20 @@ struct Dev {
   }
 };
 
+// Binary sidecar (--sidecar): full-precision copies of the outputs the text files
+// round to 6 digits.  Little-endian: "VISS" magic, uint32 version 1, uint32 type
+// (1 = complex64 pairs, 2 = float32), uint32 reserved, int64 count, then the data.
+int write_sidecar(const std::string& path, const float* data, int64_t count, uint32_t type) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return 1;
+  const uint32_t hdr[4] = {0x53534956u /* "VISS" */, 1u, type, 0u};
+  const size_t per = type == 1 ? 2 : 1;
+  bool ok = std::fwrite(hdr, sizeof(hdr), 1, f) == 1 && std::fwrite(&count, sizeof(count), 1, f) == 1 &&
+            (count == 0 || std::fwrite(data, sizeof(float) * per, (size_t)count, f) == (size_t)count);
+  ok = (std::fclose(f) == 0) && ok;
+  return ok ? 0 : 1;
+}
+
 double now() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -302,6 +316,16 @@ int vissgen(const Args& a, bool tenM) {
       std::vector<float> re(X);
       for (int64_t c = 0; c < X; ++c) re[c] = F[2 * ((int64_t)NX[c] - 1)];
       CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
+    }
+    if (a.get("sidecar", "0") != "0") {
+      // V (which the reference never writes) and complex F at full precision, next to the text file
+      std::vector<float> Vh(2 * K);
+      CHECKC(cudaMemcpy(Vh.data(), dV.p, sizeof(float) * 2 * K, cudaMemcpyDeviceToHost));
+      const std::string stem = out.substr(0, out.size() - 4);
+      if (write_sidecar(stem + ".V.c64", Vh.data(), K, 1) || write_sidecar(stem + ".F.c64", F.data(), J, 1)) {
+        std::fprintf(stderr, "cannot write the sidecar files %s.{V,F}.c64\n", stem.c_str());
+        return 1;
+      }
     }
     const double t4 = now();
     std::printf("Period %d Load UWV Cost Time is: %f s\n", p + 1, t1 - t0);

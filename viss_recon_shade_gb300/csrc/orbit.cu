@@ -9,7 +9,7 @@
 // baseline of a snapshot.  The FP32 mode evaluates the reference's float
 // formulas operation by operation (including its double-precision pieces), so
 // it reproduces the reference kernels' positions; the FP64 mode gives
-// continuous positions for the spec configurations.
+// continuous positions for the continuous-uvw (geometric-mask) configurations.
 #include <cub/cub.cuh>
 
 #include <vector>
