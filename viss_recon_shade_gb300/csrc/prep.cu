@@ -182,8 +182,9 @@ __global__ void prep_rows_kernel(RowPrepArgs a, bool recon) {
     }
   }
   a.rows0[pr] = make_int4((int)(long long)Uu, (int)(long long)Uv, (int)(long long)Uw, (int)bias);
-  a.rows1[pr] = make_float4((float)fu, (float)fv, (float)fw, c);
-  if (a.uf) a.uf[pr] = make_float4((float)Uu, (float)Uv, (float)Uw, 0.f);
+  // the FP32 parts of the phase are summed in radians: coefficients times 2 pi
+  a.rows1[pr] = make_float4((float)(fu * (double)K2PI), (float)(fv * (double)K2PI), (float)(fw * (double)K2PI), c);
+  if (a.uf) a.uf[pr] = make_float4((float)(Uu * (double)K2PI), (float)(Uv * (double)K2PI), (float)(Uw * (double)K2PI), 0.f);
   if (a.win) {
     int4 wv = recon ? make_int4(0, 0, 0, 0) : make_int4(1, 0, 0, 0);  // empty
     if (a.shade) {

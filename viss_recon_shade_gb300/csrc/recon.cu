@@ -7,7 +7,7 @@
 // in registers) against one segment of visibility rows of one channel, streamed
 // through shared memory in tiles of REC_Q.  The phase of y_k is folded into the
 // row's fixed-point bias (y e^{ix} = |y| e^{i(x + arg y)}), so a term is the
-// same as in the vis kernel: 3 IMAD [+4 FFMA fractional uvw] [+3 FFMA
+// same as in the vis kernel: 3 IMAD [+3 FFMA fractional uvw] [+3 FFMA
 // compensated], turns -> angle, __sincosf, 2 FFMA with |y_k|.
 // Masks:
 //   GEOMETRIC: rows come in snapshot runs; per run every thread tests its pixels
@@ -35,13 +35,10 @@ __device__ __forceinline__ void rec_term(const int4& r0, const float4& r1, const
                                          float& fi) {
   const uint32_t q = (uint32_t)r0.x * (uint32_t)A + (uint32_t)r0.y * (uint32_t)B + (uint32_t)r0.z * (uint32_t)C +
                      (uint32_t)r0.w;
-  float x = turns_to_angle(q);
-  if (FRAC || COMP) {
-    float d = 0.f;
-    if (FRAC) d = fmaf(r1.x, X, fmaf(r1.y, Y, r1.z * Z));
-    if (COMP) d = fmaf(rf.x, lx, fmaf(rf.y, ly, fmaf(rf.z, lz, d)));
-    x = fmaf(d, K2PI, x);
-  }
+  float e = KM3PI;
+  if (FRAC) e = fmaf(r1.x, X, fmaf(r1.y, Y, fmaf(r1.z, Z, e)));
+  if (COMP) e = fmaf(rf.x, lx, fmaf(rf.y, ly, fmaf(rf.z, lz, e)));
+  const float x = turns_to_angle(q, e);
   float sn, cs;
   __sincosf(x, &sn, &cs);
   fr = fmaf(c, cs, fr);

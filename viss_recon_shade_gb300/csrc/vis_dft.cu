@@ -7,7 +7,7 @@
 // shared memory in tiles of VIS_P pixels; every thread reads each pixel record
 // as a broadcast.  Per term:
 //   3 IMAD (phase mod 1 turn in 32-bit fixed point; exact for integer uvw)
-//   [+4 FFMA for fractional uvw] [+3 FFMA compensation]
+//   [+3 FFMA for fractional uvw] [+3 FFMA compensation]
 //   shift/or + 1 FFMA (turns -> angle), __sincosf (2 SFU ops), 2 FFMA (MAC).
 // The occlusion predicate is evaluated inline per tile:
 //   GEOMETRIC: pixels are classified against a cone bounding the shadow cones
@@ -28,13 +28,16 @@ __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const flo
                                          float WF, float& ar, float& ai) {
   const uint32_t q = (uint32_t)U * (uint32_t)a.x + (uint32_t)V * (uint32_t)a.y + (uint32_t)W * (uint32_t)a.z +
                      (uint32_t)bias;
-  float x = turns_to_angle(q);
+  float x;
   if (FRAC || COMP) {
-    // fractional uvw [and the pixel fixed-point rounding], in FP32, added to the angle
-    float d = 0.f;
-    if (FRAC) d = fmaf(FU, __int_as_float(b.x), fmaf(FV, __int_as_float(b.y), FW * __int_as_float(b.z)));
-    if (COMP) d = fmaf(UF, lo.x, fmaf(VF, lo.y, fmaf(WF, lo.z, d)));
-    x = fmaf(d, K2PI, x);
+    // fractional uvw [and the pixel fixed-point rounding], in FP32 radians (the row
+    // coefficients carry the 2 pi), summed onto the angle's constant
+    float e = KM3PI;
+    if (FRAC) e = fmaf(FU, __int_as_float(b.x), fmaf(FV, __int_as_float(b.y), fmaf(FW, __int_as_float(b.z), e)));
+    if (COMP) e = fmaf(UF, lo.x, fmaf(VF, lo.y, fmaf(WF, lo.z, e)));
+    x = turns_to_angle(q, e);
+  } else {
+    x = turns_to_angle(q, KM3PI);
   }
   float sn, cs;
   __sincosf(x, &sn, &cs);

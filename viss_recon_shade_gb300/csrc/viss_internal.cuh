@@ -97,17 +97,20 @@ enum PixClass : int { CLS_VIS = 0, CLS_OCC = 1, CLS_MIX = 2 };
 // Phase (turns * 2^32, mod 2^32) = U*A + V*B + W*C + bias_k; bias_k carries
 // PHASE_BIAS, f_w*s*n_offset and (reconstruction) the phase of the row's
 // visibility.  The fractional part delta = f_u*x + f_v*y + f_w*z' (FP32, z' = s*n,
-// |delta| <= 0.87 turn) and the compensation terms are added to the FP32 angle
-// with one FFMA after the fixed-point turn has been converted.
+// |delta| <= 0.87 turn) and the compensation terms are evaluated in radians (the
+// row coefficients carry the 2 pi) on top of the angle's constant, and enter with
+// the FFMA that converts the fixed-point turn.
 __device__ __forceinline__ uint32_t fix32(double x) {
   return (uint32_t)(unsigned long long)llrint(x * 4294967296.0);
 }
 
-// Turns (as uint32 mod 2^32, PHASE_BIAS already added) -> angle in [-pi, pi)
-// shifted by half a turn: returns x = 2 pi (t - 1/2), so cos/sin come out negated.
-__device__ __forceinline__ float turns_to_angle(uint32_t q) {
+// Turns (as uint32 mod 2^32, PHASE_BIAS already added) -> angle shifted by half a
+// turn, x = 2 pi (t - 1/2) + (e - KM3PI), so cos/sin come out negated.  e is
+// KM3PI plus the FP32 parts of the phase in radians (fractional uvw, compensation),
+// summed onto the constant so the conversion and the addition share one FFMA.
+__device__ __forceinline__ float turns_to_angle(uint32_t q, float e) {
   const float f = __uint_as_float((q >> 9) | 0x3f800000u);
-  return fmaf(f, K2PI, KM3PI);
+  return fmaf(f, K2PI, e);
 }
 
 // Satellite indices of a visibility (geometric mask): gm = snapshot*nsat + m in the
