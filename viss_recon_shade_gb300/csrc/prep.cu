@@ -358,6 +358,66 @@ int launch_prep_rowblock_cones(const int* rowsat, const float4* satdir, const Ch
   return VISS_OK;
 }
 
+// Bounding cone of each block of `block` consecutive sky positions (unit
+// directions in pgeo): axis = normalised mean, radius r = largest angle from it,
+// widened by 1e-6.  {axis, cos r}, {sin r}; cos r = -2 when the block has no axis.
+__global__ void block_cones_kernel(const float4* pgeo, int64_t J, int block, float4* cones) {
+  __shared__ double red[3][32];
+  __shared__ double axis[3];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const int64_t j0 = (int64_t)blockIdx.x * block;
+  int64_t j1 = j0 + block;
+  if (j1 > J) j1 = J;
+  double sx = 0, sy = 0, sz = 0;
+  for (int64_t j = j0 + tid; j < j1; j += blockDim.x) {
+    const float4 g = pgeo[j];
+    sx += g.x; sy += g.y; sz += g.z;
+  }
+  for (int o = 16; o; o >>= 1) {
+    sx += __shfl_xor_sync(0xffffffffu, sx, o);
+    sy += __shfl_xor_sync(0xffffffffu, sy, o);
+    sz += __shfl_xor_sync(0xffffffffu, sz, o);
+  }
+  if (lane == 0) { red[0][wid] = sx; red[1][wid] = sy; red[2][wid] = sz; }
+  __syncthreads();
+  if (tid == 0) {
+    double a = 0, b = 0, c = 0;
+    for (int w = 0; w < nw; ++w) { a += red[0][w]; b += red[1][w]; c += red[2][w]; }
+    const double nn = sqrt(a * a + b * b + c * c);
+    axis[0] = nn > 1e-3 ? a / nn : 0.0; axis[1] = nn > 1e-3 ? b / nn : 0.0; axis[2] = nn > 1e-3 ? c / nn : 0.0;
+  }
+  __syncthreads();
+  double mc = 2.0;
+  for (int64_t j = j0 + tid; j < j1; j += blockDim.x) {
+    const float4 g = pgeo[j];
+    mc = fmin(mc, axis[0] * g.x + axis[1] * g.y + axis[2] * g.z);
+  }
+  for (int o = 16; o; o >>= 1) mc = fmin(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+  __syncthreads();
+  if (lane == 0) red[0][wid] = mc;
+  __syncthreads();
+  if (tid == 0) {
+    for (int w = 0; w < nw; ++w) mc = fmin(mc, red[0][w]);
+    const bool ok = (axis[0] != 0.0 || axis[1] != 0.0 || axis[2] != 0.0) && mc <= 1.0 && mc > -1.0;
+    double cr = -2.0, sr = 1.0;
+    if (ok) {
+      const double r = acos(fmin(1.0, mc)) + 1e-6;
+      cr = cos(r);
+      sr = sin(r);
+    }
+    cones[2 * blockIdx.x] = make_float4((float)axis[0], (float)axis[1], (float)axis[2], (float)cr);
+    cones[2 * blockIdx.x + 1] = make_float4((float)sr, 0.f, 0.f, 0.f);
+  }
+}
+
+int launch_prep_block_cones(const float4* pgeo, int64_t J, int block, int64_t nblocks, float4* cones,
+                            cudaStream_t st) {
+  if (nblocks <= 0) return VISS_OK;
+  block_cones_kernel<<<(unsigned)nblocks, 256, 0, st>>>(pgeo, J, block, cones);
+  VISS_LAUNCH_CHECK("block_cones_kernel");
+  return VISS_OK;
+}
+
 struct SnapMember {
   int64_t base;
   __device__ int operator()(int64_t i) const { return (int)(base + i); }

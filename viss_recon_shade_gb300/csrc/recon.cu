@@ -61,6 +61,7 @@ struct RecSmem {
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
   float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
   int srange[2];
+  int wkeep[REC_THREADS / 32];
   float4 acc[REC_PIX];            // running totals (re, im) and their Kahan compensation per pixel
 };
 
@@ -99,13 +100,64 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
   int64_t jlast = jfirst + REC_PIX - 1;
   if (jlast > p.J - 1) jlast = p.J - 1;
 
+  // geometric: the block's bounding cone {axis, cos r, sin r}; a row whose snapshot
+  // hides every pixel of the block is dropped from the tile, for all warps at once
+  float4 bc0 = make_float4(0.f, 0.f, 0.f, -2.f);
+  float bsin = 1.f;
+  if (RM == RM_GEO) {
+    bc0 = __ldg(p.bcones + 2 * pb);
+    bsin = __ldg(p.bcones + 2 * pb + 1).x;
+  }
+
   for (int64_t tile = kb; tile < ke; tile += REC_Q) {
-    const int nq = (int)((ke - tile) < REC_Q ? (ke - tile) : REC_Q);
+    int nq = (int)((ke - tile) < REC_Q ? (ke - tile) : REC_Q);
     __syncthreads();
     if (RM == RM_GEO && tid == 0) { sm.srange[0] = 0x7fffffff; sm.srange[1] = -1; }
-    if (RM == RM_GEO) __syncthreads();
+    if (RM == RM_GEO) {
+      // keep row tid unless its snapshot's all-occluded cone {a, cos ao} holds the whole
+      // block: angle(axis, a) + r < ao, i.e. axis.a > cos(ao - r) = cos ao cos r + sin ao sin r
+      bool keep = false;
+      int pk = 0;
+      if (tid < nq) {
+        pk = p.rowsat[tile + tid];
+        const int sn = sat_gm(pk) / p.nsat;
+        const float4 sc = __ldg(p.scones + 2 * (int64_t)sn);
+        keep = true;
+        if (sc.w <= 1.f && bc0.w >= -1.f && sc.w < bc0.w) {  // the cone is wider than the block
+          const float cao = sc.w, sao = sqrtf(fmaxf(0.f, 1.f - cao * cao));
+          const float lim = fmaf(cao, bc0.w, sao * bsin) + 1e-5f;
+          const float d = fmaf(bc0.x, sc.x, fmaf(bc0.y, sc.y, bc0.z * sc.z));
+          keep = !(d > lim);
+        }
+      }
+      static_assert(REC_Q == REC_THREADS, "one row per thread in the geometric tile load");
+      const unsigned bal = __ballot_sync(0xffffffffu, keep);
+      if ((tid & 31) == 0) sm.wkeep[tid >> 5] = __popc(bal);
+      __syncthreads();
+      int off = __popc(bal & ((1u << (tid & 31)) - 1u)), tot = 0;
+#pragma unroll
+      for (int w2 = 0; w2 < REC_THREADS / 32; ++w2) {
+        const int c = sm.wkeep[w2];
+        if (w2 < (tid >> 5)) off += c;
+        tot += c;
+      }
+      if (keep) {
+        const int64_t k = tile + tid;
+        sm.r0[off] = p.rows0[k];
+        sm.r1[off] = p.rows1[k];
+        if (COMP) sm.rf[off] = p.rowsf[k];
+        const int sn = sat_gm(pk) / p.nsat;
+        sm.pk[off] = pk;
+        sm.snap[off] = sn;
+        atomicMin(&sm.srange[0], sn);
+        atomicMax(&sm.srange[1], sn);
+      }
+      nq = tot;
+      __syncthreads();
+      if (nq == 0) continue;  // the block is hidden from every row of this tile
+    }
     bool hit = false;
-    for (int r = tid; r < nq; r += REC_THREADS) {
+    for (int r = tid; r < (RM == RM_GEO ? 0 : nq); r += REC_THREADS) {
       const int64_t k = tile + r;
       sm.r0[r] = p.rows0[k];
       sm.r1[r] = p.rows1[k];
@@ -117,14 +169,6 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
           const int64_t lo_idx = (int64_t)p.res + 1, hi_idx = (int64_t)wv.y * p.res + wv.x;
           if (lo_idx <= jlast && hi_idx >= jfirst) hit = true;
         }
-      }
-      if (RM == RM_GEO) {
-        const int pk = p.rowsat[k];
-        const int sn = sat_gm(pk) / p.nsat;
-        sm.pk[r] = pk;
-        sm.snap[r] = sn;
-        atomicMin(&sm.srange[0], sn);
-        atomicMax(&sm.srange[1], sn);
       }
     }
     const bool masked_tile = __syncthreads_or(hit) != 0;

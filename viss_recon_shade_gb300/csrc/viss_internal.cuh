@@ -263,6 +263,7 @@ struct ReconParams {
   const int4* win;
   const float4* satdir;
   const float4* scones;   // [S*2] per-snapshot cones
+  const float4* bcones;   // [npb*2] bounding cone of each pixel block: {axis, cos r}, {sin r}
   const float* l;
   const float* m;
   const float* n;
@@ -311,6 +312,7 @@ int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satd
 int launch_prep_rowblock_cones(const int* rowsat, const float4* satdir, const ChannelRows& ch, int64_t nblocks,
                                float4* cones, cudaStream_t st);
 int launch_prep_snapshot_cones(const float4* satdir, int64_t S, int nsat, float4* cones, cudaStream_t st);
+int launch_prep_block_cones(const float4* pgeo, int64_t J, int block, int64_t nblocks, float4* cones, cudaStream_t st);
 
 // Persistent launches: ctas_per_sm 0 = as many as fit.
 int launch_vis_fast(const VisParams& p, int ctas_per_sm, bool compensated, cudaStream_t st);
