@@ -64,7 +64,7 @@ class Batch(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("ctas_per_sm", C.c_int32), ("vis_split", C.c_int32), ("rec_items", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("tile", C.c_int32)]
 
 
 class OrbitCfg(C.Structure):

@@ -208,9 +208,10 @@ class Tuning:
     ctas_per_sm: int = 0
     vis_split: int = 0
     rec_items: int = 0
+    tile: int = 0  # bit 0: vis sky tiles of 256 pixels; bit 1: recon row tiles of 128 visibilities
 
     def c(self) -> L.Tuning:
-        return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), 0)
+        return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), int(self.tile))
 
 
 class ChannelBatch:
@@ -311,11 +312,15 @@ class ChannelBatch:
 
 
 def tuning_candidates() -> list:
-    """Launch choices the autotuner times: persistent CTAs per SM x recon items per CTA x sky split."""
+    """Launch choices the autotuner times: tile shapes (sky tile of the vis kernel, row tile
+    of the recon kernel), persistent CTAs per SM, recon items per CTA, sky split."""
     out = []
-    for ctas in (0, 2):
-        for items in (2, 4, 8):
-            out.append(Tuning(ctas_per_sm=ctas, rec_items=items))
+    for tile in (0, 1, 2, 3):
+        for items in (16, 32):
+            out.append(Tuning(tile=tile, rec_items=items))
+    out.append(Tuning(rec_items=8))
+    out.append(Tuning(rec_items=64))
+    out.append(Tuning(ctas_per_sm=2))
     out.append(Tuning(vis_split=1))
     out.append(Tuning(vis_split=2))
     return out

@@ -48,6 +48,7 @@ struct Tuning {
   int ctas_per_sm = 0;
   int vis_split = 0;
   int rec_items = 0;
+  int tile = 0;  // bit 0: vis sky tiles of VIS_P / 2; bit 1: recon row tiles of REC_Q / 2
 };
 
 static int make_batch(const viss_batch* b, int64_t K, const viss_dft_cfg& cfg, Batch& out) {
@@ -78,6 +79,7 @@ static Tuning make_tuning(const viss_tuning* t) {
     r.ctas_per_sm = t->ctas_per_sm > 0 ? t->ctas_per_sm : 0;
     r.vis_split = t->vis_split > 0 ? t->vis_split : 0;
     r.rec_items = t->rec_items > 0 ? t->rec_items : 0;
+    r.tile = t->tile & 3;
   }
   return r;
 }
@@ -223,7 +225,9 @@ struct RecPlan {
 static void plan_segments(RecPlan& p, const Batch& bt, const Tuning& tn) {
   constexpr int64_t unit = REC_Q;
   const int nch = bt.ch.nch;
-  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 4) * planned_ctas(tn, VISS_REC_MINB);
+  // items per CTA: many short segments balance blocks whose pixels the Moon hides for
+  // different parts of the orbit (32 measured best on the 10 and 30 MHz workloads)
+  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 32) * planned_ctas(tn, VISS_REC_MINB);
   int64_t L = p.npb > 0 ? (p.K * p.npb + target - 1) / target : p.K;
   L = round_up(L > unit ? L : unit, unit);
   auto count = [&](int64_t len) {
@@ -404,8 +408,10 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   vp.K = vis.K; vp.J = sky.J; vp.jchunk = p.jchunk; vp.nsplit = p.nsplit;
   vp.nitems = (int)(p.nrb * p.nsplit);
   vp.res = cfg.res > 0 ? cfg.res : 1; vp.occ_val = cfg.occluded_value; vp.R = cfg.moon_radius_km;
+  vp.nsat = geo ? geo->nsat : 1;
   vp.mask = cfg.mask_mode;
   vp.ch = bt.ch;
+  vp.small_tile = tn.tile & 1;
   if (map) {
     vp.use_map = 1;
     vp.map.box = p.mbox; vp.map.mem = p.mmem; vp.map.members = p.members; vp.map.FF = map->FF;
@@ -508,6 +514,7 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   rp.K = vis.K; rp.J = sky.J;
   rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
   rp.recon_mask = cfg.recon_mask;
+  rp.small_tile = (tn.tile >> 1) & 1;
   rp.npb = (int)p.npb;
   rp.nseg = p.nseg;
   rp.nitems = (int)(p.nseg * p.npb);

@@ -5,7 +5,7 @@
 //
 // A work item is REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates
 // in registers) against one segment of visibility rows of one channel, streamed
-// through shared memory in tiles of REC_Q.  The phase of y_k is folded into the
+// through shared memory in tiles of REC_Q (or REC_Q / 2) rows.  The phase of y_k is folded into the
 // row's fixed-point bias (y e^{ix} = |y| e^{i(x + arg y)}), so a term is the
 // same as in the vis kernel: 3 IMAD [+3 FFMA fractional uvw] [+3 FFMA
 // compensated], turns -> angle, __sincosf, 2 FFMA with |y_k|.
@@ -49,15 +49,15 @@ constexpr int RM_NONE = 0, RM_REF = 1, RM_GEO = 2;
 constexpr int REC_SAT_CACHE = 1024;  // satellite directions cached per tile (float4)
 constexpr int REC_CONE_CACHE = 128;  // snapshot cones cached per tile
 
-template <int RM, bool COMP>
+template <int RM, bool COMP, int Q>
 struct RecSmem {
-  int4 r0[REC_Q];
-  float4 r1[REC_Q];
-  float4 rf[COMP ? REC_Q : 1];
-  int4 win[RM == RM_REF ? REC_Q : 1];
-  int pk[RM == RM_GEO ? REC_Q : 1];
-  int snap[RM == RM_GEO ? REC_Q : 1];
-  int runend[RM == RM_GEO ? REC_Q : 1];
+  int4 r0[Q];
+  float4 r1[Q];
+  float4 rf[COMP ? Q : 1];
+  int4 win[RM == RM_REF ? Q : 1];
+  int pk[RM == RM_GEO ? Q : 1];
+  int snap[RM == RM_GEO ? Q : 1];
+  int runend[RM == RM_GEO ? Q : 1];
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
   float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
   int srange[2];
@@ -65,8 +65,8 @@ struct RecSmem {
   float4 acc[REC_PIX];            // running totals (re, im) and their Kahan compensation per pixel
 };
 
-template <int RM, bool FRAC, bool COMP>
-__device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP>& sm, int64_t pb, int64_t kb,
+template <int RM, bool FRAC, bool COMP, int Q>
+__device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP, Q>& sm, int64_t pb, int64_t kb,
                                            int64_t ke, float2* out, float norm, bool direct) {
   const int tid = threadIdx.x;
   // a warp owns 32 * REC_TJ consecutive positions: with the spatial order of
@@ -109,8 +109,8 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     bsin = __ldg(p.bcones + 2 * pb + 1).x;
   }
 
-  for (int64_t tile = kb; tile < ke; tile += REC_Q) {
-    int nq = (int)((ke - tile) < REC_Q ? (ke - tile) : REC_Q);
+  for (int64_t tile = kb; tile < ke; tile += Q) {
+    int nq = (int)((ke - tile) < Q ? (ke - tile) : Q);
     __syncthreads();
     if (RM == RM_GEO && tid == 0) { sm.srange[0] = 0x7fffffff; sm.srange[1] = -1; }
     if (RM == RM_GEO) {
@@ -130,7 +130,7 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
           keep = !(d > lim);
         }
       }
-      static_assert(REC_Q == REC_THREADS, "one row per thread in the geometric tile load");
+      static_assert(Q <= REC_THREADS, "at most one row per thread in the geometric tile load");
       const unsigned bal = __ballot_sync(0xffffffffu, keep);
       if ((tid & 31) == 0) sm.wkeep[tid >> 5] = __popc(bal);
       __syncthreads();
@@ -310,9 +310,9 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
 // Persistent: grid = resident CTAs; each CTA takes the next work item (segment,
 // pixel block) from an atomic counter until none are left.  The counter is
 // reset by the host before the launch; no CTA waits on another.
-template <int RM, bool COMP>
+template <int RM, bool COMP, int Q>
 __global__ void __launch_bounds__(REC_THREADS, VISS_REC_MINB) recon_fast_kernel(const ReconParams p) {
-  __shared__ RecSmem<RM, COMP> sm;
+  __shared__ RecSmem<RM, COMP, Q> sm;
   __shared__ int s_item;
   const bool frac = __ldg(p.flags + FLAG_FRAC) != 0;
   for (;;) {
@@ -326,19 +326,26 @@ __global__ void __launch_bounds__(REC_THREADS, VISS_REC_MINB) recon_fast_kernel(
     const int ch = p.seg_ch[seg], slot = p.seg_slot[seg];
     const bool direct = slot < 0;
     float2* out = direct ? p.out + (int64_t)ch * p.J : p.partial + (int64_t)slot * p.J;
-    if (frac) recon_body<RM, true, COMP>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
-    else recon_body<RM, false, COMP>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
+    if (frac) recon_body<RM, true, COMP, Q>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
+    else recon_body<RM, false, COMP, Q>(p, sm, pb, p.seg_lo[seg], p.seg_hi[seg], out, p.ch_norm[ch], direct);
   }
 }
 
+template <int RM, bool COMP, int Q>
+static void launch_tile(const ReconParams& p, int ctas_per_sm, cudaStream_t st) {
+  const int g = persistent_grid(recon_fast_kernel<RM, COMP, Q>, REC_THREADS, ctas_per_sm, p.nitems);
+  recon_fast_kernel<RM, COMP, Q><<<g, REC_THREADS, 0, st>>>(p);
+}
+
+// Row tiles of REC_Q visibilities, or REC_Q / 2 (tuning).
 template <int RM>
 static void launch_rm(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
-  if (comp) {
-    const int g = persistent_grid(recon_fast_kernel<RM, true>, REC_THREADS, ctas_per_sm, p.nitems);
-    recon_fast_kernel<RM, true><<<g, REC_THREADS, 0, st>>>(p);
+  if (p.small_tile) {
+    if (comp) launch_tile<RM, true, REC_Q / 2>(p, ctas_per_sm, st);
+    else launch_tile<RM, false, REC_Q / 2>(p, ctas_per_sm, st);
   } else {
-    const int g = persistent_grid(recon_fast_kernel<RM, false>, REC_THREADS, ctas_per_sm, p.nitems);
-    recon_fast_kernel<RM, false><<<g, REC_THREADS, 0, st>>>(p);
+    if (comp) launch_tile<RM, true, REC_Q>(p, ctas_per_sm, st);
+    else launch_tile<RM, false, REC_Q>(p, ctas_per_sm, st);
   }
 }
 

@@ -4,7 +4,7 @@
 //
 // Tiled kernel: a work item is VIS_ROWS = 1024 visibilities of one channel (4
 // per thread, in registers) against one chunk of the sky, streamed through
-// shared memory in tiles of VIS_P pixels; every thread reads each pixel record
+// shared memory in tiles of VIS_P (or VIS_P / 2) pixels; every thread reads each pixel record
 // as a broadcast.  Per term:
 //   3 IMAD (phase mod 1 turn in 32-bit fixed point; exact for integer uvw)
 //   [+3 FFMA for fractional uvw] [+3 FFMA compensation]
@@ -119,22 +119,22 @@ __device__ __forceinline__ float ref_map_value(const FineMapDev& m, const int4& 
   return ref_members_value(m, wv, j, res, occ);
 }
 
-template <int MASK, bool COMP>
+template <int MASK, bool COMP, int P>
 struct VisSmem {
   static constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
   static constexpr bool REF = MASK == VISS_MASK_REF_QUIRK || MASK == VISS_MASK_REF_INTENDED;
-  int4 p0[VIS_P];
-  int4 p1[VIS_P];
-  float4 lo[COMP ? VIS_P : 1];
-  float4 geo[GEO ? VIS_P : 1];
-  int2 qr[REF ? VIS_P : 1];
+  int4 p0[P];
+  int4 p1[P];
+  float4 lo[COMP ? P : 1];
+  float4 geo[GEO ? P : 1];
+  int2 qr[REF ? P : 1];
   int4 win[REF ? VIS_ROWS : 1];   // the block's REF windows, read in masked tiles only
   int wcnt[VIS_THREADS / 32][2];
   float4 acc[VIS_ROWS];           // running totals (re, im) and their Kahan compensation per visibility
 };
 
-template <int MASK, bool FRAC, bool COMP>
-__device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>& sm, int64_t rb, int split, int ch,
+template <int MASK, bool FRAC, bool COMP, int P>
+__device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP, P>& sm, int64_t rb, int split, int ch,
                                          int64_t rb_first, int64_t row_first, int64_t nvalid) {
   constexpr bool GEO = MASK == VISS_MASK_GEOMETRIC;
   constexpr bool REF = MASK == VISS_MASK_REF_QUIRK || MASK == VISS_MASK_REF_INTENDED;
@@ -191,8 +191,8 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
   int64_t je = jb + p.jchunk;
   if (je > p.J) je = p.J;
 
-  for (int64_t tile = jb; tile < je; tile += VIS_P) {
-    const int np = (int)((je - tile) < VIS_P ? (je - tile) : VIS_P);
+  for (int64_t tile = jb; tile < je; tile += P) {
+    const int np = (int)((je - tile) < P ? (je - tile) : P);
     __syncthreads();  // previous tile fully consumed
 #pragma unroll
     for (int i = 0; i < VIS_TK; ++i) tr[i] = ti[i] = 0.f;
@@ -201,7 +201,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
     if (GEO) {
       // pass 1: classify against the block's bounding cone (only the class is
       // kept across the barrier); pass 2: re-read the records (L2) and place them.
-      constexpr int Q = VIS_P / VIS_THREADS;
+      constexpr int Q = P / VIS_THREADS;
       unsigned cls = 0;  // 2 bits per slot: 1 fast, 2 mixed
 #pragma unroll
       for (int qq = 0; qq < Q; ++qq) {
@@ -243,7 +243,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
           const float4 g = p.pgeo[j];
           const float d = fmaf(g.x, cone0.x, fmaf(g.y, cone0.y, g.z * cone0.z));
           if (c == 1u && d > cone0.w) a.w = __float_as_int(occ_val);
-          const int pos = c == 1u ? offF + __popc(bF[qq] & lt) : VIS_P - 1 - (offM + __popc(bM[qq] & lt));
+          const int pos = c == 1u ? offF + __popc(bF[qq] & lt) : P - 1 - (offM + __popc(bM[qq] & lt));
           s_p0[pos] = a;
           if (FRAC) s_p1[pos] = p.pix1[j];
           if (COMP) s_lo[pos] = p.plo[j];
@@ -332,7 +332,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
         gn[i] = sat_gn(pk);
       }
       for (int mi = 0; mi < nmix; ++mi) {
-        const int pi = VIS_P - 1 - mi;
+        const int pi = P - 1 - mi;
         const int4 a = s_p0[pi];
         int4 b = make_int4(0, 0, 0, 0);
         float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -382,9 +382,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP>
 // pixel chunk) from an atomic counter until none are left, so uneven items
 // (channels, occluded fractions) balance without a wave tail.  The counter is
 // reset by the host before the launch; no CTA ever waits on another.
-template <int MASK, bool COMP>
+template <int MASK, bool COMP, int P>
 __global__ void __launch_bounds__(VIS_THREADS, VISS_VIS_MINB) vis_fast_kernel(const VisParams p) {
-  __shared__ VisSmem<MASK, COMP> sm;
+  __shared__ VisSmem<MASK, COMP, P> sm;
   __shared__ int s_item;
   const bool frac = __ldg(p.flags + FLAG_FRAC) != 0;
   for (;;) {
@@ -398,20 +398,28 @@ __global__ void __launch_bounds__(VIS_THREADS, VISS_VIS_MINB) vis_fast_kernel(co
     int ch = 0;
     while (ch + 1 < p.ch.nch && rb >= p.ch.rb_off[ch + 1]) ++ch;
     const int64_t nvalid = p.ch.row_off[ch + 1] - p.ch.row_off[ch];
-    if (frac) vis_body<MASK, true, COMP>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
-    else vis_body<MASK, false, COMP>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
+    if (frac) vis_body<MASK, true, COMP, P>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
+    else vis_body<MASK, false, COMP, P>(p, sm, rb, split, ch, p.ch.rb_off[ch], p.ch.row_off[ch], nvalid);
   }
 }
 
 // Persistent grid: resident CTAs of this kernel (capped by ctas_per_sm) on every SM.
+template <int MASK, bool COMP, int P>
+static void launch_tile(const VisParams& p, int ctas_per_sm, cudaStream_t st) {
+  const int g = persistent_grid(vis_fast_kernel<MASK, COMP, P>, VIS_THREADS, ctas_per_sm, p.nitems);
+  vis_fast_kernel<MASK, COMP, P><<<g, VIS_THREADS, 0, st>>>(p);
+}
+
+// Sky tile of VIS_P pixels, or VIS_P / 2 (tuning): smaller tiles halve the shared
+// memory per block and the granularity of the occlusion compaction.
 template <int MASK>
 static void launch_mask(const VisParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
-  if (comp) {
-    const int g = persistent_grid(vis_fast_kernel<MASK, true>, VIS_THREADS, ctas_per_sm, p.nitems);
-    vis_fast_kernel<MASK, true><<<g, VIS_THREADS, 0, st>>>(p);
+  if (p.small_tile) {
+    if (comp) launch_tile<MASK, true, VIS_P / 2>(p, ctas_per_sm, st);
+    else launch_tile<MASK, false, VIS_P / 2>(p, ctas_per_sm, st);
   } else {
-    const int g = persistent_grid(vis_fast_kernel<MASK, false>, VIS_THREADS, ctas_per_sm, p.nitems);
-    vis_fast_kernel<MASK, false><<<g, VIS_THREADS, 0, st>>>(p);
+    if (comp) launch_tile<MASK, true, VIS_P>(p, ctas_per_sm, st);
+    else launch_tile<MASK, false, VIS_P>(p, ctas_per_sm, st);
   }
 }
 

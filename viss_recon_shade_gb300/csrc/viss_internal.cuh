@@ -81,7 +81,7 @@ constexpr int REC_Q = 256;                // visibilities per shared-memory tile
 // Channels of one batched pass, and visibility segments of its reconstruction
 // (their tables travel in the kernel parameters).
 constexpr int VISS_MAX_CH = VISS_MAX_CHANNELS;
-constexpr int VISS_MAX_SEG = 96;
+constexpr int VISS_MAX_SEG = 256;
 
 // Geometric test: |e| below this margin is re-decided in double.
 constexpr float GEO_EPS = 2e-6f;
@@ -239,6 +239,7 @@ struct VisParams {
   int nsplit;
   int nitems;             // work items (rowblock, pixel chunk) = nrb * nsplit
   int res;
+  int nsat;               // satellites per snapshot (geometric)
   float occ_val;
   double R;
   int mask;               // VISS_MASK_*
@@ -248,6 +249,7 @@ struct VisParams {
   // k's window (vissGen10M_shade.cu:120-136)
   FineMapDev map;
   int use_map;            // 0: identity map
+  int small_tile;         // sky tiles of VIS_P / 2 pixels
 };
 
 struct ReconParams {
@@ -285,6 +287,7 @@ struct ReconParams {
   int64_t seg_lo[VISS_MAX_SEG], seg_hi[VISS_MAX_SEG];
   int seg_ch[VISS_MAX_SEG], seg_slot[VISS_MAX_SEG];   // slot -1: the segment writes F directly
   float ch_norm[VISS_MAX_CH];
+  int small_tile;         // tiles of REC_Q / 2 visibility rows
 };
 
 // Per-channel sum of partial slots (channels split into several segments).
