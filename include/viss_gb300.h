@@ -136,9 +136,11 @@ VISS_API int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const vi
  * take cudaMalloc's synchronisation -- and that do not want to pass a
  * workspace either.  Same arguments and result as viss_vis_dft; the scratch is
  * a VISS_NOALLOC_SCRATCH_BYTES array inside the library, resident on every GPU
- * that loads it.  Passes whose viss_vis_dft_workspace() exceeds that size are
- * rejected with VISS_ERR_RANGE (131,072 visibilities x 196,608 pixels with the
- * geometric mask fit; the full 1,835,008 x 196,608 workload does not).  The first call on a device looks up the array's
+ * that loads it.  It splits the sky into fewer chunks than viss_vis_dft (its
+ * partial sums are the largest part of the scratch); passes that still need more
+ * than the scratch are rejected with VISS_ERR_RANGE (131,072 visibilities x
+ * 196,608 pixels with the geometric mask fit; the full 1,835,008 x 196,608
+ * workload does not).  The first call on a device looks up the array's
  * device address; make it before any stream capture.  Calls share the array:
  * calls that overlap on the GPU race. */
 #define VISS_NOALLOC_SCRATCH_BYTES (32u << 20)

@@ -154,12 +154,13 @@ static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64
   p.nrb = bt.ch.rb_off[bt.ch.nch];
   p.Kpad = (p.nrb > 0 ? p.nrb : 1) * VIS_ROWS;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
-  // Split the pixel axis when the visibility blocks alone give fewer than ~4
-  // work items per resident CTA.
+  // Split the sky into chunks until there are ~32 work items (visibility block x
+  // sky chunk) per resident CTA: blocks see different occluded fractions of the sky,
+  // and short items balance them (10 MHz vis: 1 chunk 158 ms, 2 149 ms, 16 143 ms).
   const int64_t slots = planned_ctas(tn, VISS_VIS_MINB);
   int64_t nsplit = 1;
   if (tn.vis_split > 0) nsplit = tn.vis_split;
-  else if (p.nrb > 0 && p.nrb < 4 * slots) nsplit = (4 * slots + p.nrb - 1) / p.nrb;
+  else if (p.nrb > 0 && p.nrb < 32 * slots) nsplit = (32 * slots + p.nrb - 1) / p.nrb;
   const int64_t maxsplit = (J + VIS_P - 1) / VIS_P;
   if (nsplit > maxsplit) nsplit = maxsplit;
   if (nsplit < 1) nsplit = 1;
@@ -226,8 +227,8 @@ static void plan_segments(RecPlan& p, const Batch& bt, const Tuning& tn) {
   constexpr int64_t unit = REC_Q;
   const int nch = bt.ch.nch;
   // items per CTA: many short segments balance blocks whose pixels the Moon hides for
-  // different parts of the orbit (32 measured best on the 10 and 30 MHz workloads)
-  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 32) * planned_ctas(tn, VISS_REC_MINB);
+  // different parts of the orbit (10 MHz recon: 4 items 191 ms, 8 176 ms, 32 167 ms, 64 165 ms)
+  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 64) * planned_ctas(tn, VISS_REC_MINB);
   int64_t L = p.npb > 0 ? (p.K * p.npb + target - 1) / target : p.K;
   L = round_up(L > unit ? L : unit, unit);
   auto count = [&](int64_t len) {

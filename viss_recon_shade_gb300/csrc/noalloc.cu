@@ -51,10 +51,20 @@ int scratch_address(void** out) {
 
 using namespace viss;
 
+// Few sky chunks: their partial sums (chunks x K complex values) are the largest
+// part of the scratch.  ~4 work items per resident CTA.
+static viss_tuning noalloc_tuning(int64_t K) {
+  viss_tuning t{};
+  const int64_t nrb = (K + VIS_ROWS - 1) / VIS_ROWS, slots = (int64_t)device_sm_count() * VISS_VIS_MINB;
+  t.vis_split = (nrb > 0 && nrb < 4 * slots) ? (int32_t)((4 * slots + nrb - 1) / nrb) : 1;
+  return t;
+}
+
 extern "C" int viss_vis_dft_noalloc(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
                                     const viss_geometry* geo, float* V, void* stream) {
   if (!cfg || !sky || !vis) return fail(VISS_ERR_INVALID, "cfg, sky or vis is NULL");
-  const size_t need = viss_vis_dft_workspace(cfg, vis->K, sky->J, geo);
+  const viss_tuning tn = noalloc_tuning(vis->K);
+  const size_t need = viss_vis_dft_batch_workspace(cfg, nullptr, vis->K, sky->J, geo, &tn);
   if (need > (size_t)VISS_NOALLOC_SCRATCH_BYTES)
     return fail(VISS_ERR_RANGE, "viss_vis_dft_noalloc: this pass needs " + std::to_string(need) +
                                     " bytes of scratch, more than the built-in " +
@@ -64,5 +74,5 @@ extern "C" int viss_vis_dft_noalloc(const viss_dft_cfg* cfg, const viss_sky* sky
   int rc = scratch_address(&scratch);
   if (rc) return rc;
   // the same checks and pass as viss_vis_dft, on the built-in scratch
-  return viss_vis_dft(cfg, sky, vis, geo, V, scratch, (size_t)VISS_NOALLOC_SCRATCH_BYTES, stream);
+  return viss_vis_dft_batch(cfg, sky, vis, nullptr, geo, &tn, V, scratch, (size_t)VISS_NOALLOC_SCRATCH_BYTES, stream);
 }
