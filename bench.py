@@ -36,7 +36,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gterms/s shaded vis-DFT + recon, 1 GB300, chosen vs plain at ≤1e-5 rel err"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
 # capture of this workload at full size (the command is kept with the ncu summaries).
-TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 110.97e6, "recon_fast_kernel": 123.49e6}}
+TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 199.07e6, "recon_fast_kernel": 293.82e6}}
 UNIT = "Gterms/s"
 L2_FLUSH_BYTES = 256 << 20
 
@@ -588,6 +588,54 @@ def batch_accuracy(d, b, cfg):
             "recon_rms": float(np.linalg.norm(Fg - Fo) / np.linalg.norm(Fo))}
 
 
+# ------------------------------------------------------------------ stage 1: orbits -> uvw
+def run_stage1(args, ws, rank, local):
+    """--workload stage1: the reference's uvw generation at its own size
+    (MIncline_generate_uvw_float.cu: 8 satellites, OrbitRes 864,000, 140 orbits,
+    10 MHz): windowed satellite positions, ceil((x_n - x_m) 1e3 / lambda) for the 56
+    ordered pairs of 40.32M snapshots = 2.26e9 uvw, then the sort + unique.
+    Reported: uvw rows per second through the three stages (positions, baselines,
+    dedup), inputs generated on the device."""
+    import torch
+    import viss_recon_shade_gb300 as V
+    cfg = V.OrbitConfig()  # the reference's constants
+    st = torch.cuda.current_stream()
+
+    def step():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(st)
+        pos = V.orbit_positions(cfg)
+        ev[1].record(st)
+        u, v, w, snap, pair = V.baseline_uvw(pos, 30.0, ordered=True, rounding=True)
+        del snap, pair, pos
+        ev[2].record(st)
+        uu, vv, ww = V.dedup_uvw(u, v, w)
+        ev[3].record(st)
+        torch.cuda.synchronize()
+        n = uu.numel()
+        K = u.numel()
+        del u, v, w, uu, vv, ww
+        torch.cuda.empty_cache()
+        return K, n, [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+
+    for _ in range(args.warmup):
+        step()
+    res = [step() for _ in range(args.steps)]
+    K, n = res[0][0], res[0][1]
+    ms = [sum(r[2][i] for r in res) / len(res) for i in range(3)]
+    total = sum(ms)
+    line = {"metric": "uvw rows/s, orbit positions + baseline uvw + sort/unique, 1 GB300",
+            "value": round(K / (total * 1e-3) / 1e9, 3), "unit": "G uvw rows/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 positions, int64 keys", "data": "generated on the device",
+            "config": {"workload": "stage1", "nsat": cfg.nsat, "orbit_res": cfg.orbit_res,
+                       "orbit_counts": cfg.orbit_counts, "snapshots": cfg.snapshots, "uvw_rows": K,
+                       "unique_rows": n, "freq_hz": 1e7},
+            "stage_ms": {"positions": round(ms[0], 2), "baselines": round(ms[1], 2), "dedup": round(ms[2], 2)}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     ws, rank, local = dist_setup()
@@ -596,6 +644,8 @@ def main():
         run_reference(args, ws, rank, local)
     elif args.workload in BATCH_WORKLOADS:
         run_batch(args, ws, rank, local)
+    elif args.workload == "stage1":
+        run_stage1(args, ws, rank, local)
     else:
         run_ours(args, ws, rank, local)
     if ws > 1:
