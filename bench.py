@@ -261,11 +261,24 @@ def run_ours(args, ws, rank, local):
     dom_ms, dom = (vis_ms, "vis_fast_kernel") if vis_ms >= rec_ms else (rec_ms, "recon_fast_kernel")
     achieved = 2.0 * K * J / (dom_ms * 1e-3) / 1e9
     props = torch.cuda.get_device_properties(0)
+    traffic = TRAFFIC_BYTES.get(wl.name, {}).get(dom)
+    hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
+    try:
+        hbm_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+        hbm_src = "MEASURED_PEAKS.json hbm_gbs (measured copy bandwidth)"
+    except Exception:
+        pass
+    hbm = None
+    if traffic:
+        gbs = traffic / (dom_ms * 1e-3) / 1e9
+        hbm = {"achieved": round(gbs, 2), "peak": hbm_peak, "unit": "GB/s", "frac": round(gbs / hbm_peak, 5),
+               "peak_source": hbm_src}
+    # the path is bound by the SFU (sin, cos per term), not by HBM or the tensor cores
     roofline = {"bound": "sfu", "kernel": dom, "achieved": round(achieved, 2), "peak": round(sfu_peak, 2),
                 "unit": "G SFU op/s", "frac": round(achieved / sfu_peak, 4),
                 "peak_source": "measured: viss_sfu_probe (8 independent __sincosf chains per thread) in this run",
                 "algorithmic_per_term": "2 SFU ops (sin, cos) + 6 FMA-pipe ops (vis) / 8 (recon)",
-                "traffic": TRAFFIC_BYTES.get(wl.name, {}).get(dom), "traffic_unit": "bytes per launch (ncu)",
+                "traffic": traffic, "traffic_unit": "bytes per launch (ncu)", "hbm": hbm,
                 "sm_count": props.multi_processor_count,
                 "vis_ms": round(vis_ms, 3), "recon_ms": round(rec_ms, 3)}
 

@@ -225,8 +225,8 @@ typedef struct viss_batch {
  * autotuner times candidates on the caller's own data and picks one. */
 typedef struct viss_tuning {
   int32_t ctas_per_sm;       /* persistent CTAs per SM (0: as many as fit) */
-  int32_t vis_split;         /* sky chunks per visibility block, each a work item (0: enough for ~4 items per CTA) */
-  int32_t rec_items;         /* recon work items per persistent CTA the row segments aim at (0: 32) */
+  int32_t vis_split;         /* sky chunks per visibility block, each a work item (0: enough for ~32 items per CTA) */
+  int32_t rec_items;         /* recon work items per persistent CTA the row segments aim at (0: 64) */
   int32_t tile;              /* tile shapes: bit 0 vis sky tiles of 256 pixels (else 512),
                                 bit 1 recon row tiles of 128 visibilities (else 256) */
 } viss_tuning;

@@ -1,0 +1,76 @@
+"""Stage 1 of the path, the inputs of the DFT: baseline uvw
+(MIncline_generate_uvw_float.cu:149-164, computeUVW: ceil((x_n - x_m) * 1e3 / lambda)
+in double) and the sort + unique of the uvw rows (:60-71 SortCompare, :352-356).
+
+baseline_uvw: bit-exact against the oracle's double arithmetic, on positions
+  chosen so that many quotients land within a few ulp of an integer (where the
+  kernel's reciprocal product has to give way to the division).
+dedup_uvw: the same unique rows, in the same order, as the oracle's sort +
+  unique, on the hash path (many repeats), on the sort fallback (a table that
+  fills up) and on small inputs; the first occurrence's values are kept
+  (-0 before +0 stays -0); non-integer input is rejected on both paths."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def V():
+    import viss_recon_shade_gb300 as V
+    return V
+
+
+@pytest.mark.parametrize("lam", [10.0, 29.0, 1.0 / 3.0])
+@pytest.mark.parametrize("rounding", [True, False])
+def test_baseline_uvw_bit_exact(V, oracle, lam, rounding):
+    rng = np.random.default_rng(int(lam * 7) + rounding)
+    S, nsat = 400, 8
+    # positions on a 0.01 km (10 m) grid: (x_n - x_m) * 1e3 / lambda sits near integers
+    pos = (rng.integers(-300000, 300000, (S, nsat, 3)) * 0.01).astype(np.float32)
+    pos[::7] = rng.normal(0, 2000, (len(pos[::7]), nsat, 3)).astype(np.float32)
+    u, v, w, snap, pair = V.baseline_uvw(torch.from_numpy(pos).cuda(), lam, ordered=True, rounding=rounding)
+    uo, vo, wo, so, po = oracle.uvw(pos, lam, ordered=True, rounding=rounding)
+    for g, o in ((u, uo), (v, vo), (w, wo)):
+        assert np.array_equal(g.cpu().numpy().view(np.int32), o.view(np.int32))
+    assert np.array_equal(snap.cpu().numpy(), so) and np.array_equal(pair.cpu().numpy(), po)
+
+
+def dedup_case(rng, K, nkeys, span=3000):
+    keys = rng.integers(-span, span, (nkeys, 3)).astype(np.float32)
+    pick = rng.integers(0, nkeys, K)
+    return [np.ascontiguousarray(keys[pick, i]) for i in range(3)]
+
+
+@pytest.mark.parametrize("K,nkeys", [(300_000, 5_000), (2_000_000, 400_000), (5_000, 50_000), (3_000, 800),
+                                     (1, 1)])
+def test_dedup_matches_oracle(V, oracle, K, nkeys):
+    rng = np.random.default_rng(K + nkeys)
+    u, v, w = dedup_case(rng, K, nkeys)
+    g = V.dedup_uvw(*(torch.from_numpy(x).cuda() for x in (u, v, w)))
+    o = oracle.dedup_uvw(u, v, w)
+    for a, b in zip(g, o):
+        assert np.array_equal(a.cpu().numpy(), b)
+
+
+@pytest.mark.parametrize("K", [8_000, 600])  # hash path, sort path
+def test_dedup_keeps_first_occurrence(V, K):
+    rng = np.random.default_rng(3)
+    u, v, w = dedup_case(rng, K, 200)
+    u[:4] = [-0.0, 0.0, 0.0, -0.0]  # rows (+-0, 1, 2) then (+-0, 5, 5)
+    v[:4] = [1, 1, 5, 5]
+    w[:4] = [2, 2, 5, 5]
+    uu, vv, ww = (x.cpu().numpy() for x in V.dedup_uvw(*(torch.from_numpy(x).cuda() for x in (u, v, w))))
+    i = np.nonzero((uu == 0) & (vv == 1) & (ww == 2))[0]
+    j = np.nonzero((uu == 0) & (vv == 5) & (ww == 5))[0]
+    assert len(i) == 1 and len(j) == 1
+    assert np.signbit(uu[i[0]]) and not np.signbit(uu[j[0]])
+
+
+@pytest.mark.parametrize("K", [8_000, 600])
+def test_dedup_rejects_non_integer(V, K):
+    u, v, w = dedup_case(np.random.default_rng(4), K, 100)
+    u[K // 2] = 0.5
+    with pytest.raises(RuntimeError):
+        V.dedup_uvw(*(torch.from_numpy(x).cuda() for x in (u, v, w)))

@@ -142,25 +142,44 @@ __device__ __forceinline__ void pair_of(int q, int nsat, int ordered, int* m, in
   }
 }
 
+// ceil((double)diff * 1e3 / lambda) rounded to float, as computeUVW evaluates it
+__device__ __noinline__ float ceil_quotient_exact(float diff, double lambda) {
+  return (float)ceil((double)diff * 1e3 / lambda);
+}
+
 __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64_t S, int nsat, int ordered, int npairs,
-                                    double lambda, int rounding, float* u, float* v, float* w, int32_t* snap,
-                                    int32_t* pair) {
+                                    uint64_t pair_magic, double lambda, float scale32, int rounding, float* u,
+                                    float* v, float* w, int32_t* snap, int32_t* pair) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S * npairs) return;
-  const int64_t g = k / npairs;
-  const int q = (int)(k % npairs);
+  // k / npairs by a multiply-high (magic = ceil(2^64 / npairs)), corrected once
+  int64_t g = (int64_t)__umul64hi((uint64_t)k, pair_magic);
+  int q = (int)(k - g * npairs);
+  if (q < 0) { --g; q += npairs; }
+  if (q >= npairs) { ++g; q -= npairs; }
   int m, n;
   pair_of(q, nsat, ordered, &m, &n);
   float out[3];
   for (int c = 0; c < 3; ++c) {
-    double x;
     if (pos64) {
-      x = (pos64[(g * nsat + n) * 3 + c] - pos64[(g * nsat + m) * 3 + c]) * 1e3 / lambda;
-    } else {
-      const float diff = pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c];
-      x = (double)diff * 1e3 / lambda;  // computeUVW (:156-158)
+      const double x = (pos64[(g * nsat + n) * 3 + c] - pos64[(g * nsat + m) * 3 + c]) * 1e3 / lambda;
+      out[c] = rounding ? (float)ceil(x) : (float)x;
+      continue;
     }
-    out[c] = rounding ? (float)ceil(x) : (float)x;
+    const float diff = pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c];
+    if (!rounding) {
+      out[c] = (float)((double)diff * 1e3 / lambda);  // computeUVW without the ceil
+      continue;
+    }
+    // computeUVW (:156-158): ceil((double)diff * 1e3 / lambda).  The FP32 product
+    // x = diff * fl(1e3 / lambda) is within 2^-23 |x| of the quotient; where x lies
+    // more than 2^-21 |x| inside (n, n + 1) the quotient and its double rounding
+    // do too, so ceilf(x) is the same integer (and sign of zero).  Elsewhere, and
+    // for |x| >= 2^22 where x - floor(x) stops being exact, divide in double.
+    const float x = diff * scale32;
+    const float f = x - floorf(x);
+    const float tol = fabsf(x) * 4.76837158203125e-7f + 1e-30f;
+    out[c] = (fabsf(x) < 4194304.f && f > tol && 1.f - f > tol) ? ceilf(x) : ceil_quotient_exact(diff, lambda);
   }
   u[k] = out[0]; v[k] = out[1]; w[k] = out[2];
   if (snap) snap[k] = (int32_t)g;
@@ -195,6 +214,66 @@ __global__ void dedup_gather_kernel(const uint64_t* keys, const uint32_t* idx, i
   ou[k] = u[s]; ov[k] = v[s]; ow[k] = w[s];
 }
 
+// Hash pass: the unique keys of the input with the first row index of each, in
+// an open-addressing table (linear probing, at most DEDUP_PROBES slots per key;
+// a key that finds no slot sets overflow and the caller falls back to sorting
+// every row).  Most rows repeat a key already present: they cost a read and,
+// when they come earlier than the recorded row, an atomicMin.
+constexpr uint64_t DEDUP_EMPTY = ~0ull;
+constexpr int DEDUP_PROBES = 256;
+
+__device__ __forceinline__ uint64_t dedup_hash(uint64_t k) {  // splitmix64 finaliser
+  k ^= k >> 30; k *= 0xbf58476d1ce4e5b9ull;
+  k ^= k >> 27; k *= 0x94d049bb133111ebull;
+  return k ^ (k >> 31);
+}
+
+__global__ void dedup_hash_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* tkeys,
+                                  uint32_t* tidx, uint64_t mask, int* bad, int* overflow) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  const float c[3] = {u[k], v[k], w[k]};
+  uint64_t key = 0;
+  for (int i = 0; i < 3; ++i) {
+    const float x = c[i];
+    if (!(x == rintf(x)) || !(fabsf(x) < 1048576.f)) { atomicOr(bad, 1); }
+    const int64_t q = (int64_t)x + 1048576;
+    key = (key << 21) | ((uint64_t)q & 0x1fffff);
+  }
+  uint64_t h = dedup_hash(key) & mask;
+  for (int probe = 0; probe < DEDUP_PROBES; ++probe, h = (h + 1) & mask) {
+    uint64_t cur = *((volatile uint64_t*)(tkeys + h));
+    if (cur == DEDUP_EMPTY) {
+      cur = atomicCAS((unsigned long long*)(tkeys + h), (unsigned long long)DEDUP_EMPTY, (unsigned long long)key);
+      if (cur == DEDUP_EMPTY) cur = key;
+    }
+    if (cur == key) {
+      if (*((volatile uint32_t*)(tidx + h)) > (uint32_t)k) atomicMin(tidx + h, (uint32_t)k);
+      return;
+    }
+  }
+  atomicOr(overflow, 1);
+}
+
+__global__ void dedup_table_init_kernel(uint64_t* tkeys, uint32_t* tidx, int64_t n) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) { tkeys[t] = DEDUP_EMPTY; tidx[t] = 0xffffffffu; }
+}
+
+__global__ void dedup_occupied_kernel(const uint64_t* tkeys, int64_t n, int* flag) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) flag[t] = tkeys[t] != DEDUP_EMPTY;
+}
+
+// sorted unique rows -> u, v, w (the first occurrence's values)
+__global__ void dedup_emit_kernel(const uint32_t* idx, const int64_t* n, const float* u, const float* v,
+                                  const float* w, float* ou, float* ov, float* ow) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *n) return;
+  const uint32_t s = idx[k];
+  ou[k] = u[s]; ov[k] = v[s]; ow[k] = w[s];
+}
+
 struct DedupPlan {
   uint64_t *k0 = nullptr, *k1 = nullptr;
   uint32_t *i0 = nullptr, *i1 = nullptr;
@@ -217,7 +296,14 @@ struct DedupPlan {
                                     (uint32_t*)nullptr, (int64_t)K, 0, 63);
     cub::DeviceSelect::Flagged(nullptr, b, (float*)nullptr, (int*)nullptr, (float*)nullptr, (int64_t*)nullptr,
                                (int64_t)K);
+    size_t c2 = 0, c3 = 0;
+    cub::DeviceSelect::Flagged(nullptr, c2, (uint64_t*)nullptr, (int*)nullptr, (uint64_t*)nullptr,
+                               (int64_t*)nullptr, (int64_t)K);
+    cub::DeviceSelect::Flagged(nullptr, c3, (uint32_t*)nullptr, (int*)nullptr, (uint32_t*)nullptr,
+                               (int64_t*)nullptr, (int64_t)K);
     cub_bytes = a > b ? a : b;
+    if (c2 > cub_bytes) cub_bytes = c2;
+    if (c3 > cub_bytes) cub_bytes = c3;
     cub = c.take<char>(cub_bytes);
     bytes = c.size();
   }
@@ -282,8 +368,9 @@ int viss_baseline_uvw(const float* pos, const double* pos64, int64_t S, int32_t 
   const int64_t K = S * npairs;
   if (K == 0) return VISS_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  baseline_uvw_kernel<<<(unsigned)((K + 255) / 256), 256, 0, st>>>(pos, pos64, S, nsat, ordered, npairs, lambda_m,
-                                                                  rounding, u, v, w, snap, pair);
+  const uint64_t magic = ~0ull / (uint64_t)npairs + 1;
+  baseline_uvw_kernel<<<(unsigned)((K + 255) / 256), 256, 0, st>>>(
+      pos, pos64, S, nsat, ordered, npairs, magic, lambda_m, (float)(1e3 / lambda_m), rounding, u, v, w, snap, pair);
   VISS_LAUNCH_CHECK("baseline_uvw_kernel");
   return VISS_OK;
 }
@@ -309,6 +396,49 @@ int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   VISS_CUDA(cudaMemsetAsync(p.bad, 0, 4 * sizeof(int), st));
   const unsigned nb = (unsigned)((K + 255) / 256);
+  // Hash pass first, in the sort path's buffers: a table of T slots (keys in k0,
+  // first indices in i0; T <= K, the buffers' length), from 2^25 slots up to 2^28
+  // while it fills up.  The occupied slots (unique keys and their first rows) are
+  // compacted into k1/i1, sorted by key back into k0/i0 and emitted.  A table that
+  // stays full leaves the work to the sort over every row below.
+  for (int64_t T = (int64_t)1 << 25, prev = 0; K >= 4096; prev = T, T <<= 3) {
+    while (T > K) T >>= 1;
+    if (T <= prev) break;
+    dedup_table_init_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(p.k0, p.i0, T);
+    VISS_LAUNCH_CHECK("dedup_table_init_kernel");
+    dedup_hash_kernel<<<nb, 256, 0, st>>>(u, v, w, K, p.k0, p.i0, (uint64_t)(T - 1), p.bad, p.bad + 1);
+    VISS_LAUNCH_CHECK("dedup_hash_kernel");
+    int hb[2] = {0, 0};
+    VISS_CUDA(cudaMemcpyAsync(hb, p.bad, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    VISS_CUDA(cudaStreamSynchronize(st));
+    if (hb[0]) return fail(VISS_ERR_RANGE, "dedup needs integer-valued uvw with |x| < 2^20");
+    if (!hb[1]) {
+      dedup_occupied_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(p.k0, T, p.flag);
+      VISS_LAUNCH_CHECK("dedup_occupied_kernel");
+      size_t cb = p.cub_bytes;
+      VISS_CUDA(cub::DeviceSelect::Flagged(p.cub, cb, p.k0, p.flag, p.k1, p.nsel, T, st));
+      cb = p.cub_bytes;
+      VISS_CUDA(cub::DeviceSelect::Flagged(p.cub, cb, p.i0, p.flag, p.i1, p.nsel, T, st));
+      int64_t n = 0;
+      VISS_CUDA(cudaMemcpyAsync(&n, p.nsel, sizeof(n), cudaMemcpyDeviceToHost, st));
+      VISS_CUDA(cudaStreamSynchronize(st));
+      // unique keys: the sort's stability does not matter
+      cb = p.cub_bytes;
+      VISS_CUDA(cub::DeviceRadixSort::SortPairs(p.cub, cb, p.k1, p.k0, p.i1, p.i0, n, 0, 63, st));
+      if (n > 0) {
+        dedup_emit_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p.i0, p.nsel, u, v, w, p.tu, p.tv, p.tw);
+        VISS_LAUNCH_CHECK("dedup_emit_kernel");
+        VISS_CUDA(cudaMemcpyAsync(u, p.tu, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        VISS_CUDA(cudaMemcpyAsync(v, p.tv, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+        VISS_CUDA(cudaMemcpyAsync(w, p.tw, sizeof(float) * n, cudaMemcpyDeviceToDevice, st));
+      }
+      VISS_CUDA(cudaStreamSynchronize(st));
+      *count_out = n;
+      return VISS_OK;
+    }
+    VISS_CUDA(cudaMemsetAsync(p.bad, 0, 4 * sizeof(int), st));
+    if (T >= ((int64_t)1 << 28)) break;
+  }
   dedup_keys_kernel<<<nb, 256, 0, st>>>(u, v, w, K, p.k0, p.i0, p.bad);
   VISS_LAUNCH_CHECK("dedup_keys_kernel");
   // stable radix sort: among equal keys the first input occurrence stays first
