@@ -607,36 +607,52 @@ def run_stage1(args, ws, rank, local):
     (MIncline_generate_uvw_float.cu: 8 satellites, OrbitRes 864,000, 140 orbits,
     10 MHz): windowed satellite positions, ceil((x_n - x_m) 1e3 / lambda) for the 56
     ordered pairs of 40.32M snapshots = 2.26e9 uvw, then the sort + unique.
-    Reported: uvw rows per second through the three stages (positions, baselines,
-    dedup), inputs generated on the device."""
+    Timed: positions + the fused baselines/unique pass (viss_unique_uvw).  The
+    two-call path (viss_baseline_uvw + viss_dedup_uvw, 2.26e9 rows written and
+    read back; the pair-major transpose between them untimed) is timed once
+    afterwards, checked against the fused result and reported beside it.
+    Reported: uvw rows per second, inputs generated on the device."""
     import torch
     import viss_recon_shade_gb300 as V
     cfg = V.OrbitConfig()  # the reference's constants
     st = torch.cuda.current_stream()
+    lam = 30.0
 
     def step():
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         ev[0].record(st)
         pos = V.orbit_positions(cfg)
         ev[1].record(st)
-        u, v, w, snap, pair = V.baseline_uvw(pos, 30.0, ordered=True, rounding=True)
-        del snap, pair, pos
+        uu, vv, ww = V.unique_uvw(pos, lam, ordered=True, capacity=1 << 25)
         ev[2].record(st)
-        uu, vv, ww = V.dedup_uvw(u, v, w)
-        ev[3].record(st)
         torch.cuda.synchronize()
         n = uu.numel()
-        K = u.numel()
-        del u, v, w, uu, vv, ww
-        torch.cuda.empty_cache()
-        return K, n, [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+        K = pos.shape[0] * pos.shape[1] * (pos.shape[1] - 1)
+        return K, n, [ev[i].elapsed_time(ev[i + 1]) for i in range(2)], (pos, uu, vv, ww)
 
     for _ in range(args.warmup):
         step()
     res = [step() for _ in range(args.steps)]
     K, n = res[0][0], res[0][1]
-    ms = [sum(r[2][i] for r in res) / len(res) for i in range(3)]
+    ms = [sum(r[2][i] for r in res) / len(res) for i in range(2)]
     total = sum(ms)
+    # the two-call path once, on the last step's positions, checked against the fused result
+    pos, uu, vv, ww = res[-1][3]
+    del res
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(st)
+    u, v, w, snap, pair = V.baseline_uvw(pos, lam, ordered=True, rounding=True)
+    del snap, pair
+    ev[1].record(st)
+    # the reference's pair-major concatenation, as viss_unique_uvw ranks first occurrences
+    u, v, w = (x.view(pos.shape[0], -1).t().contiguous().view(-1) for x in (u, v, w))
+    u2, v2, w2 = V.dedup_uvw(u, v, w)
+    ev[2].record(st)
+    torch.cuda.synchronize()
+    same = all(torch.equal(a.view(torch.int32), b.view(torch.int32)) for a, b in ((uu, u2), (vv, v2), (ww, w2)))
+    two = [ev[i].elapsed_time(ev[i + 1]) for i in range(2)]
+    del u, v, w, u2, v2, w2
+    torch.cuda.empty_cache()
     line = {"metric": "uvw rows/s, orbit positions + baseline uvw + sort/unique, 1 GB300",
             "value": round(K / (total * 1e-3) / 1e9, 3), "unit": "G uvw rows/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total, 2), "higher_is_better": True, "scaling": "weak",
@@ -644,7 +660,8 @@ def run_stage1(args, ws, rank, local):
             "config": {"workload": "stage1", "nsat": cfg.nsat, "orbit_res": cfg.orbit_res,
                        "orbit_counts": cfg.orbit_counts, "snapshots": cfg.snapshots, "uvw_rows": K,
                        "unique_rows": n, "freq_hz": 1e7},
-            "stage_ms": {"positions": round(ms[0], 2), "baselines": round(ms[1], 2), "dedup": round(ms[2], 2)}}
+            "stage_ms": {"positions": round(ms[0], 2), "unique_fused": round(ms[1], 2)},
+            "two_call_ms": {"baselines": round(two[0], 2), "dedup": round(two[1], 2), "identical": same}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

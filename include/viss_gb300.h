@@ -297,6 +297,19 @@ VISS_API int viss_baseline_uvw(const float* pos, const double* pos64, int64_t S,
 VISS_API size_t viss_dedup_uvw_workspace(int64_t K);
 VISS_API int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, void* workspace,
                    size_t workspace_bytes, void* stream);
+/* The uvw generation of MIncline_generate_uvw_float.cu:341-397 in one pass that never
+ * materialises the S x pairs rows: viss_baseline_uvw (float positions, ceil), the rows
+ * concatenated pair-major as the reference does, then viss_dedup_uvw.  The unique rows in
+ * SortCompare order, each with the values of its first occurrence (lowest pair, then
+ * earliest snapshot: the sign of a zero coordinate).  Rows repeated from the previous
+ * snapshot of the same pair skip the hash table.  u, v, w receive up to `capacity` rows; *count_out (HOST) the unique
+ * count (the call synchronises the stream).  capacity 0 only counts; a smaller nonzero
+ * capacity than the count returns VISS_ERR_RANGE with the count set.  More unique rows
+ * than the internal table holds (~2^28) return VISS_ERR_RANGE: use the two calls then. */
+VISS_API size_t viss_unique_uvw_workspace(int64_t S, int32_t nsat, int ordered);
+VISS_API int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int ordered, double lambda_m, float* u,
+                    float* v, float* w, int64_t capacity, int64_t* count_out, void* workspace,
+                    size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------- shade windows */
 /* Cart2SphKernel + mean radius + ShadeMatrix (shade1M.cu:62-105, 218-225).

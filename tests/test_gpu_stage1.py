@@ -74,3 +74,39 @@ def test_dedup_rejects_non_integer(V, K):
     u[K // 2] = 0.5
     with pytest.raises(RuntimeError):
         V.dedup_uvw(*(torch.from_numpy(x).cuda() for x in (u, v, w)))
+
+
+def pair_major(pos, x):
+    """snapshot-major rows [S * P] -> the reference's pair-major concatenation"""
+    return x.view(pos.shape[0], -1).t().reshape(-1)
+
+
+@pytest.mark.parametrize("ordered", [True, False])
+def test_unique_uvw_equals_two_calls(V, oracle, ordered):
+    """The fused pass against baseline_uvw + the pair-major concatenation +
+    dedup_uvw (bit-exact, sign of zero included) and the oracle (values), on
+    windowed orbit positions whose pairs repeat keys over runs of snapshots, with
+    run boundaries inside the data."""
+    cfg = V.OrbitConfig(orbit_res=7200, orbit_counts=3)
+    pos = V.orbit_positions(cfg)
+    for lam in (30.0, 3.0):
+        u, v, w, _, _ = V.baseline_uvw(pos, lam, ordered=ordered, rounding=True)
+        ref = V.dedup_uvw(*(pair_major(pos, x) for x in (u, v, w)))
+        got = V.unique_uvw(pos, lam, ordered=ordered, capacity=64)  # short capacity: the retry path
+        for a, b in zip(got, ref):
+            assert np.array_equal(a.cpu().numpy().view(np.int32), b.cpu().numpy().view(np.int32))
+        o = oracle.dedup_uvw(u.cpu().numpy(), v.cpu().numpy(), w.cpu().numpy())
+        for a, b in zip(got, o):
+            assert np.array_equal(a.cpu().numpy(), b)
+
+
+def test_unique_uvw_random_positions(V):
+    """Positions without run structure (every row inserts) and S not a multiple of
+    the run length."""
+    rng = np.random.default_rng(9)
+    pos = torch.from_numpy(rng.normal(0, 50, (1003, 6, 3)).astype(np.float32)).cuda()
+    u, v, w, _, _ = V.baseline_uvw(pos, 10.0, ordered=True, rounding=True)
+    ref = V.dedup_uvw(*(pair_major(pos, x) for x in (u, v, w)))
+    got = V.unique_uvw(pos, 10.0, ordered=True)
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.cpu().numpy().view(np.int32), b.cpu().numpy().view(np.int32))

@@ -113,6 +113,9 @@ _SIGS = {
                                     _P]),
     "viss_dedup_uvw_workspace": (C.c_size_t, [C.c_int64]),
     "viss_dedup_uvw": (C.c_int, [_P, _P, _P, C.c_int64, C.POINTER(C.c_int64), _P, C.c_size_t, _P]),
+    "viss_unique_uvw_workspace": (C.c_size_t, [C.c_int64, C.c_int32, C.c_int]),
+    "viss_unique_uvw": (C.c_int, [_P, C.c_int64, C.c_int32, C.c_int, C.c_double, _P, _P, _P, C.c_int64,
+                                  C.POINTER(C.c_int64), _P, C.c_size_t, _P]),
     "viss_shade_windows_workspace": (C.c_size_t, [C.c_int64]),
     "viss_shade_windows": (C.c_int, [_P, _P, _P, C.c_int64, C.c_int, C.c_double, _P, C.POINTER(C.c_double), _P,
                                      C.c_size_t, _P]),

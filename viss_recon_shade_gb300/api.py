@@ -486,6 +486,30 @@ def dedup_uvw(u: torch.Tensor, v: torch.Tensor, w: torch.Tensor):
     return u[:n], v[:n], w[:n]
 
 
+def unique_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, capacity: int = 1 << 22):
+    """baseline_uvw (ceil) + dedup_uvw fused: the unique uvw rows of all (snapshot, pair)
+    baselines of float positions [S, nsat, 3], sorted, with the values of each key's first
+    occurrence in pair-major order (the reference's concatenation of per-pair lists).  Starts
+    with room for `capacity` rows and repeats the pass once with the exact count if that
+    is short."""
+    pos = pos.contiguous()
+    S, nsat = pos.shape[0], pos.shape[1]
+    nb = L.lib.viss_unique_uvw_workspace(S, nsat, int(ordered))
+    ws = _workspace(nb, pos.device)
+    cnt = C.c_int64(0)
+    for _ in range(2):
+        u, v, w = (torch.empty(max(capacity, 1), dtype=torch.float32, device=pos.device) for _ in range(3))
+        rc = L.lib.viss_unique_uvw(_ptr(pos), S, nsat, int(ordered), float(lambda_m), _ptr(u), _ptr(v), _ptr(w),
+                                   capacity, C.byref(cnt), _ptr(ws), nb, _stream())
+        if rc == L.VISS_ERR_RANGE and cnt.value > capacity:
+            capacity = cnt.value
+            continue
+        L.check(rc, "viss_unique_uvw")
+        n = cnt.value
+        return u[:n], v[:n], w[:n]
+    raise RuntimeError("viss_unique_uvw: unique count changed between passes")
+
+
 def shade_windows(u, v, w, RES: int, mean_r_km: float = 0.0):
     """Raw shadeM windows int32[K, 4] (1-based) and the mean radius used."""
     K = u.numel()

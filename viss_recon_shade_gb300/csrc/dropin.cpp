@@ -402,31 +402,24 @@ int mincline(const Args& a) {
     const int64_t S = viss_orbit_snapshots(&cfg);
     const int P = 56;
     const int64_t K = S * P;
-    Dev<float> pos, u, v, w, pu, pv, pw;
+    Dev<float> pos, u, v, w;
     Dev<char> ws;
-    if (pos.alloc(S * 8 * 3) || u.alloc(K) || v.alloc(K) || w.alloc(K) || pu.alloc(K) || pv.alloc(K) || pw.alloc(K)) {
+    if (pos.alloc(S * 8 * 3)) {
       std::fprintf(stderr, "device allocation failed\n");
       return 1;
     }
     CHECKV(viss_orbit_positions(&cfg, pos.p, nullptr, nullptr));
-    CHECKV(viss_baseline_uvw(pos.p, nullptr, S, 8, 1, (double)lambda, 1, u.p, v.p, w.p, nullptr, nullptr, nullptr));
-    // the reference concatenates the pairs' lists (pair-major) before its global sort
-    for (int q = 0; q < P; ++q) {
-      CHECKC(cudaMemcpy2D(pu.p + q * S, sizeof(float), u.p + q, sizeof(float) * P, sizeof(float), S,
-                          cudaMemcpyDeviceToDevice));
-      CHECKC(cudaMemcpy2D(pv.p + q * S, sizeof(float), v.p + q, sizeof(float) * P, sizeof(float), S,
-                          cudaMemcpyDeviceToDevice));
-      CHECKC(cudaMemcpy2D(pw.p + q * S, sizeof(float), w.p + q, sizeof(float) * P, sizeof(float), S,
-                          cudaMemcpyDeviceToDevice));
-    }
-    const size_t wsb = viss_dedup_uvw_workspace(K);
+    // baselines, the pairs' lists concatenated pair-major, global sort + unique, in one pass
+    const size_t wsb = viss_unique_uvw_workspace(S, 8, 1);
     if (ws.alloc(wsb)) return 1;
     int64_t cnt = 0;
-    CHECKV(viss_dedup_uvw(pu.p, pv.p, pw.p, K, &cnt, ws.p, wsb, nullptr));
+    CHECKV(viss_unique_uvw(pos.p, S, 8, 1, (double)lambda, nullptr, nullptr, nullptr, 0, &cnt, ws.p, wsb, nullptr));
+    if (u.alloc(cnt > 0 ? cnt : 1) || v.alloc(cnt > 0 ? cnt : 1) || w.alloc(cnt > 0 ? cnt : 1)) return 1;
+    CHECKV(viss_unique_uvw(pos.p, S, 8, 1, (double)lambda, u.p, v.p, w.p, cnt, &cnt, ws.p, wsb, nullptr));
     std::vector<float> h(3 * cnt);
-    CHECKC(cudaMemcpy(h.data(), pu.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
-    CHECKC(cudaMemcpy(h.data() + cnt, pv.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
-    CHECKC(cudaMemcpy(h.data() + 2 * cnt, pw.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    CHECKC(cudaMemcpy(h.data(), u.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    CHECKC(cudaMemcpy(h.data() + cnt, v.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
+    CHECKC(cudaMemcpy(h.data() + 2 * cnt, w.p, sizeof(float) * cnt, cudaMemcpyDeviceToHost));
     const std::string out = dir + "uvw" + std::to_string(index) + "frequency10M.txt";
     CHECKV(viss_text_write_floats(out.c_str(), 3, h.data(), cnt, cnt));
     std::printf("period %d: %lld unique uvw of %lld -> %s\n", index, (long long)cnt, (long long)K, out.c_str());

@@ -18,11 +18,30 @@
 
 namespace viss {
 
+// x / d for 0 <= x < 2^62 by a multiply-high with magic = ceil(2^64 / d),
+// corrected by one step either way
+struct FastDiv {
+  int64_t d = 1;
+  uint64_t magic = 0;
+  void set(int64_t dd) { d = dd; magic = dd > 1 ? ~0ull / (uint64_t)dd + 1 : 0; }
+  __device__ __forceinline__ int64_t div(int64_t x) const {
+    if (d == 1) return x;
+    int64_t q = (int64_t)__umul64hi((uint64_t)x, magic);
+    const int64_t r = x - q * d;
+    if (r < 0) --q;
+    else if (r >= d) ++q;
+    return q;
+  }
+};
+
 struct OrbitDev {
   int nsat, orbit_res, orbit_counts, index;
   int span, interval;
-  int64_t total, S;
+  int64_t total, S, half, reset_index;
+  FastDiv by_span, by_res, by_nsat;
   float a, e, incl, argp, d2r;
+  double dm_den;                 // (double)(2a) * 1e3, the divisor of calculate_dM
+  float dm_hi, dm_lo, dm_inv;    // dm_den = dm_hi + dm_lo exactly; dm_inv = fl(1 / dm_den)
   double a64, e64, incl64, argp64, raan_step;
   float step_mt;
   int fp64;
@@ -36,12 +55,12 @@ struct OrbitDev {
 // satellite's slot, not yet computed when uvwPosition runs for this satellite
 // (:224-308), so it reads zero as well.
 __device__ __forceinline__ int window_index(const OrbitDev& o, int64_t g, int64_t* circle) {
-  const int64_t k = g / o.span + 1;
+  const int64_t k = o.by_span.div(g) + 1;
   const int64_t offset = (k - 1) * o.interval;
   int64_t endIdx = (k - 1) * o.orbit_res + offset + o.span;
   int64_t startIdx = (k - 1) * o.orbit_res + offset;
   if ((k - 1) * (int64_t)(o.orbit_res + o.interval) > o.total) {
-    const int64_t reset_index = o.total / (o.orbit_res + o.interval) + 1;
+    const int64_t reset_index = o.reset_index;  // total / (orbit_res + interval) + 1
     startIdx = (k - 1 - reset_index) * o.orbit_res + offset;
     endIdx = (k - 1 - reset_index) * o.orbit_res + offset + o.span;
   }
@@ -54,24 +73,83 @@ __device__ __forceinline__ int window_index(const OrbitDev& o, int64_t g, int64_
   return 0;
 }
 
-// calculateOrbit (:83-110) in the reference's arithmetic.
-__device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, float* out) {
-  const int64_t half = o.total / 2;
-  const int k = (int)(idx / o.orbit_res), po = (int)(idx % o.orbit_res);
+// calculate_dM (:51-58): (float)(asin((double)d / ((double)(2a) * 1e3)) * 2)
+__device__ __noinline__ float dm_exact(float d, double den) { return (float)(asin((double)d / den) * 2); }
+
+// The same value without FP64 for |x| = |d / den| <= 0.05.  x = xh + xl to
+// 2^-44 |x| (the FMA residual d - xh * dm_hi is exact); asin(x) = x + c,
+// c = x^3 (1/6 + 3x^2/40 + 15x^4/336 + 105x^6/3456) + x^2 xl / 2 evaluated in
+// FP32 (series tail < 2^-48 |x|; rounding < 2^-21 |c| <= 2^-23.6 x^2 |x|), and
+// hi + lo = xh + (xl + c) by Fast2Sum.  The reference rounds 2 asin(x) (double,
+// within 2^-50 |x|) to float: 2 hi is that float unless x could lie within
+// E = |hi| (x^2 2^-23 + 2^-42) of a rounding boundary, i.e. unless |lo| + E reaches
+// half the spacing to hi's nearer neighbour.  Those values, a few in 10^4, divide
+// and take asin in double.
+__device__ __forceinline__ float dm_value(const OrbitDev& o, float d) {
+  if (d == 0.f) return d;  // asin(+-0) * 2 = +-0
+  const float xh = __fmul_rn(d, o.dm_inv);
+  const float r = __fmaf_rn(-xh, o.dm_hi, d);
+  const float r2 = __fmaf_rn(-xh, o.dm_lo, r);
+  const float xl = __fmul_rn(r2, o.dm_inv);
+  const float x2 = __fmul_rn(xh, xh);
+  float P = __fmaf_rn(105.f / 3456.f, x2, 15.f / 336.f);
+  P = __fmaf_rn(P, x2, 3.f / 40.f);
+  P = __fmaf_rn(P, x2, 1.f / 6.f);
+  const float c = __fmul_rn(__fmul_rn(x2, xh), P);
+  const float S = __fadd_rn(__fadd_rn(xl, c), __fmul_rn(__fmul_rn(0.5f, x2), xl));
+  const float hi = __fadd_rn(xh, S);
+  const float lo = __fsub_rn(S, __fsub_rn(hi, xh));
+  const float ah = fabsf(hi);
+  const int bits = __float_as_int(ah);
+  const float half_gap = 0.5f * fminf(__int_as_float(bits + 1) - ah, ah - __int_as_float(bits - 1));
+  const float E = ah * __fmaf_rn(x2, 0x1p-23f, 0x1p-42f);
+  if (fabsf(xh) <= 0.05f && __fadd_rn(fabsf(lo), E) < half_gap) return 2.f * hi;
+  return dm_exact(d, o.dm_den);
+}
+
+// RAAN of orbit k (:88-89) in the reference's mixed float/double arithmetic;
+// base = (index - 1) * orbit_counts.  One compiled copy serves the per-block
+// table and the positions outside it.
+__device__ __noinline__ float raan_of(int k, int base, float d2r, double step) {
+  return (float)((double)((float)k * d2r) * step + 0.0 + (double)((float)base * d2r) * step);
+}
+
+constexpr int RAAN_TAB = 4;  // orbits per block with a precomputed RAAN
+
+// calculateOrbit (:83-110) in the reference's arithmetic.  raan_tab holds the
+// RAAN of orbits k_base .. k_base + RAAN_TAB - 1.
+__device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const float* raan_tab, int k_base,
+                             float* out) {
+  const int64_t half = o.half;
+  const int64_t kq = o.by_res.div(idx);
+  const int k = (int)kq, po = (int)(idx - kq * o.orbit_res);
   float d;
   if (idx < half) d = fmaf(o.s1[sat], (float)idx, o.r1[sat]);   // linspace r1 -> r2 (:42-49)
   else d = fmaf(o.s2[sat], (float)(idx - half), o.r2[sat]);     // linspace r2 -> r1
-  const float dM = (float)(asin((double)d / ((double)(2 * o.a) * 1e3)) * 2);  // calculate_dM (:51-58)
-  const float raan = (float)((double)((float)k * o.d2r) * o.raan_step + 0.0 +
-                             (double)((float)((o.index - 1) * o.orbit_counts) * o.d2r) * o.raan_step);
+  const float dM = dm_value(o, d);  // calculate_dM (:51-58)
+  const int dk = k - k_base;
+  const float raan = (dk >= 0 && dk < RAAN_TAB) ? raan_tab[dk]
+                                                : raan_of(k, (o.index - 1) * o.orbit_counts, o.d2r, o.raan_step);
   // Mt[po] is rounded on its own (thrust linspace with a = 0), then dM is added
   const float M = __fmul_rn(o.step_mt, (float)po) + dM;
-  float E0 = M;
+  // Newton on Kepler's equation, at most 99 updates (:95-102).  An update is a
+  // function of E0 alone, so once E0 repeats it cycles to the last update: a
+  // fixed point stays, a 2-cycle ends on the value the parity of the updates
+  // left selects.  In FP32 a few percent of samples end in such a cycle without
+  // meeting the exit test; they leave at the repeat with the same result.
+  float E0 = M, Ep = M;
   for (int i = 1; i < 100; ++i) {
     const float M0 = E0 - o.e * sinf(E0);
     const float err = M - M0;
     if (fabsf(err) < 1e-15) break;
-    E0 = E0 + err / (1 - o.e * cosf(E0));
+    const float En = E0 + err / (1 - o.e * cosf(E0));
+    if (__float_as_int(En) == __float_as_int(E0)) break;
+    if (i >= 2 && __float_as_int(En) == __float_as_int(Ep)) {
+      if (((99 - i) & 1) == 0) E0 = En;
+      break;
+    }
+    Ep = E0;
+    E0 = En;
   }
   const float temp = tanf(E0 / 2) / sqrtf((1 - o.e) / (1 + o.e));
   const float theta = atanf(temp) * 2;
@@ -93,11 +171,18 @@ __device__ void position_f64(const OrbitDev& o, int sat, int64_t idx, double* ou
   const double dM = 2.0 * asin(d / (2.0 * o.a64 * 1e3));
   const double raan = (double)k * d2r * o.raan_step + (double)(o.index - 1) * (double)o.orbit_counts * d2r * o.raan_step;
   const double M = 2.0 * kPi / (double)(o.orbit_res - 1) * (double)po + dM;
-  double E = M;
+  double E = M, Ep = M;  // the same cycle exits as the FP32 loop
   for (int i = 1; i < 100 && o.e64 != 0.0; ++i) {
     const double err = M - (E - o.e64 * sin(E));
     if (fabs(err) < 1e-15) break;
-    E = E + err / (1.0 - o.e64 * cos(E));
+    const double En = E + err / (1.0 - o.e64 * cos(E));
+    if (__double_as_longlong(En) == __double_as_longlong(E)) break;
+    if (i >= 2 && __double_as_longlong(En) == __double_as_longlong(Ep)) {
+      if (((99 - i) & 1) == 0) E = En;
+      break;
+    }
+    Ep = E;
+    E = En;
   }
   const double theta = 2.0 * atan(tan(E / 2.0) / sqrt((1.0 - o.e64) / (1.0 + o.e64)));
   const double r = o.a64 * (1.0 - o.e64 * o.e64) / (1.0 + o.e64 * cos(theta));
@@ -108,10 +193,22 @@ __device__ void position_f64(const OrbitDev& o, int sat, int64_t idx, double* ou
 }
 
 __global__ void orbit_positions_kernel(const OrbitDev o, float* pos, double* pos64) {
+  // The block's snapshots lie on one or two orbits: their RAAN (FP64 work) is
+  // computed once per block, from the orbit of the block's first snapshot on.
+  __shared__ float raan_tab[RAAN_TAB];
+  __shared__ int k_base_s;
+  if (!o.fp64 && threadIdx.x < RAAN_TAB) {
+    int64_t c0;
+    const int kind0 = window_index(o, o.by_nsat.div((int64_t)blockIdx.x * blockDim.x), &c0);
+    const int k0 = kind0 == 0 ? (int)o.by_res.div(c0) : 0;
+    raan_tab[threadIdx.x] = raan_of(k0 + (int)threadIdx.x, (o.index - 1) * o.orbit_counts, o.d2r, o.raan_step);
+    if (threadIdx.x == 0) k_base_s = k0;
+  }
+  __syncthreads();
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= o.S * o.nsat) return;
-  const int64_t g = t / o.nsat;
-  const int sat = (int)(t % o.nsat);
+  const int64_t g = o.by_nsat.div(t);
+  const int sat = (int)(t - g * o.nsat);
   int64_t circle;
   const int kind = window_index(o, g, &circle);
   const bool zero = kind != 0;
@@ -122,7 +219,7 @@ __global__ void orbit_positions_kernel(const OrbitDev o, float* pos, double* pos
     if (pos64) { pos64[3 * t] = p[0]; pos64[3 * t + 1] = p[1]; pos64[3 * t + 2] = p[2]; }
   } else {
     float p[3] = {0.f, 0.f, 0.f};
-    if (!zero) position_f32(o, sat, circle, p);
+    if (!zero) position_f32(o, sat, circle, raan_tab, k_base_s, p);
     pos[3 * t] = p[0]; pos[3 * t + 1] = p[1]; pos[3 * t + 2] = p[2];
     if (pos64) { pos64[3 * t] = p[0]; pos64[3 * t + 1] = p[1]; pos64[3 * t + 2] = p[2]; }
   }
@@ -147,6 +244,21 @@ __device__ __noinline__ float ceil_quotient_exact(float diff, double lambda) {
   return (float)ceil((double)diff * 1e3 / lambda);
 }
 
+// computeUVW (:156-158) for one coordinate of a float baseline diff = x_n - x_m:
+// ceil((double)diff * 1e3 / lambda) as float, or without the ceil.  The FP32
+// product x = diff * fl(1e3 / lambda) is within 2^-23 |x| of the quotient; where
+// x lies more than 2^-21 |x| inside (n, n + 1) the quotient and its double
+// rounding do too, so ceilf(x) is the same integer (and sign of zero).
+// Elsewhere, and for |x| >= 2^22 where x - floor(x) stops being exact, the
+// quotient is taken in double.
+__device__ __forceinline__ float baseline_coord(float diff, double lambda, float scale32, int rounding) {
+  if (!rounding) return (float)((double)diff * 1e3 / lambda);
+  const float x = diff * scale32;
+  const float f = x - floorf(x);
+  const float tol = fabsf(x) * 4.76837158203125e-7f + 1e-30f;
+  return (fabsf(x) < 4194304.f && f > tol && 1.f - f > tol) ? ceilf(x) : ceil_quotient_exact(diff, lambda);
+}
+
 __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64_t S, int nsat, int ordered, int npairs,
                                     uint64_t pair_magic, double lambda, float scale32, int rounding, float* u,
                                     float* v, float* w, int32_t* snap, int32_t* pair) {
@@ -166,20 +278,7 @@ __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64
       out[c] = rounding ? (float)ceil(x) : (float)x;
       continue;
     }
-    const float diff = pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c];
-    if (!rounding) {
-      out[c] = (float)((double)diff * 1e3 / lambda);  // computeUVW without the ceil
-      continue;
-    }
-    // computeUVW (:156-158): ceil((double)diff * 1e3 / lambda).  The FP32 product
-    // x = diff * fl(1e3 / lambda) is within 2^-23 |x| of the quotient; where x lies
-    // more than 2^-21 |x| inside (n, n + 1) the quotient and its double rounding
-    // do too, so ceilf(x) is the same integer (and sign of zero).  Elsewhere, and
-    // for |x| >= 2^22 where x - floor(x) stops being exact, divide in double.
-    const float x = diff * scale32;
-    const float f = x - floorf(x);
-    const float tol = fabsf(x) * 4.76837158203125e-7f + 1e-30f;
-    out[c] = (fabsf(x) < 4194304.f && f > tol && 1.f - f > tol) ? ceilf(x) : ceil_quotient_exact(diff, lambda);
+    out[c] = baseline_coord(pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c], lambda, scale32, rounding);
   }
   u[k] = out[0]; v[k] = out[1]; w[k] = out[2];
   if (snap) snap[k] = (int32_t)g;
@@ -189,19 +288,23 @@ __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64
 // ---------------------------------------------------------------- dedup
 // Integer-valued uvw -> 63-bit key preserving the lexicographic (u, v, w)
 // order of SortCompare (:60-71); -0 and +0 share a key as they compare equal.
-__global__ void dedup_keys_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* keys,
-                                  uint32_t* idx, int* bad) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
-  const float c[3] = {u[k], v[k], w[k]};
+__device__ __forceinline__ uint64_t uvw_key(float a, float b, float c, int* bad) {
+  const float x3[3] = {a, b, c};
   uint64_t key = 0;
   for (int i = 0; i < 3; ++i) {
-    const float x = c[i];
+    const float x = x3[i];
     if (!(x == rintf(x)) || !(fabsf(x) < 1048576.f)) { atomicOr(bad, 1); }
     const int64_t q = (int64_t)x + 1048576;
     key = (key << 21) | ((uint64_t)q & 0x1fffff);
   }
-  keys[k] = key;
+  return key;
+}
+
+__global__ void dedup_keys_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* keys,
+                                  uint32_t* idx, int* bad) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  keys[k] = uvw_key(u[k], v[k], w[k], bad);
   idx[k] = (uint32_t)k;
 }
 
@@ -228,18 +331,9 @@ __device__ __forceinline__ uint64_t dedup_hash(uint64_t k) {  // splitmix64 fina
   return k ^ (k >> 31);
 }
 
-__global__ void dedup_hash_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* tkeys,
-                                  uint32_t* tidx, uint64_t mask, int* bad, int* overflow) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= K) return;
-  const float c[3] = {u[k], v[k], w[k]};
-  uint64_t key = 0;
-  for (int i = 0; i < 3; ++i) {
-    const float x = c[i];
-    if (!(x == rintf(x)) || !(fabsf(x) < 1048576.f)) { atomicOr(bad, 1); }
-    const int64_t q = (int64_t)x + 1048576;
-    key = (key << 21) | ((uint64_t)q & 0x1fffff);
-  }
+// key -> its slot (claimed if new), the slot's row index lowered to k
+__device__ __forceinline__ void dedup_insert(uint64_t* tkeys, uint32_t* tidx, uint64_t mask, uint64_t key,
+                                             uint32_t k, int* overflow) {
   uint64_t h = dedup_hash(key) & mask;
   for (int probe = 0; probe < DEDUP_PROBES; ++probe, h = (h + 1) & mask) {
     uint64_t cur = *((volatile uint64_t*)(tkeys + h));
@@ -248,21 +342,205 @@ __global__ void dedup_hash_kernel(const float* u, const float* v, const float* w
       if (cur == DEDUP_EMPTY) cur = key;
     }
     if (cur == key) {
-      if (*((volatile uint32_t*)(tidx + h)) > (uint32_t)k) atomicMin(tidx + h, (uint32_t)k);
+      if (*((volatile uint32_t*)(tidx + h)) > k) atomicMin(tidx + h, k);
       return;
     }
   }
   atomicOr(overflow, 1);
 }
 
+__global__ void dedup_hash_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* tkeys,
+                                  uint32_t* tidx, uint64_t mask, int* bad, int* overflow) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= K) return;
+  dedup_insert(tkeys, tidx, mask, uvw_key(u[k], v[k], w[k], bad), (uint32_t)k, overflow);
+}
+
+// Fused baselines + hash pass over the rows (snapshot g, pair q) of float
+// positions [S][nsat][3], ranked pair-major (row q * S + g) as the reference
+// concatenates its per-pair lists before the global sort + unique
+// (MIncline_generate_uvw_float.cu:370-397): the first occurrence of a key is its
+// lowest pair, then its earliest snapshot.  A thread walks one satellite pair m < n over UNIQUE_RUN
+// consecutive snapshots, for ordered pairs both rows (m, n) and (n, m), and
+// inserts a row only where its key differs from the previous snapshot's: an
+// equal key there has the smaller row index already.  Baselines move by far
+// less than a wavelength between snapshots, so most rows touch no table slot.
+constexpr int UNIQUE_RUN = 256;
+
+// Key fields of row (m, n) and row (n, m) for one coordinate: F = ceil(q) + 2^20
+// with q = (double)(+-diff) * 1e3 / lambda, the integers baseline_coord gives
+// (without their sign of zero).  floor(x) of x = diff * scale32 comes from the
+// round-down sum x + 1.5 * 2^23 (exact for |x| < 2^22), so ceil(x) = floor(x) + 1
+// where the fast-path test of baseline_coord holds (for -x exactly when for x),
+// and ceil(-x) = -floor(x): F(n, m) = 2^21 + 1 - F(m, n).  With |x| < 2^20 - 2 as
+// well, both fields lie in [2, 2^21 - 2] and the three fields of (n, m) are one
+// 64-bit subtraction from those of (m, n).  Returns false where the slow path
+// decides (fields then exact, or 0 with *oor set when out of |c| < 2^20).
+__device__ __forceinline__ bool coord_fields(float diff, double lambda, float scale32, uint32_t* ff, uint32_t* fr,
+                                             bool* oor) {
+  const float x = diff * scale32;
+  const float y = __fadd_rd(x, 12582912.f);
+  const float f = x - (y - 12582912.f);
+  const float ax = fabsf(x);
+  const float tol = ax * 4.76837158203125e-7f + 1e-30f;
+  if (ax < 1048574.f && f > tol && 1.f - f > tol) {
+    *ff = (uint32_t)(__float_as_int(y) - 0x4b400000 + 1 + 1048576);
+    return true;
+  }
+  const float a = ceil_quotient_exact(diff, lambda), b = ceil_quotient_exact(-diff, lambda);
+  const bool ok = fabsf(a) < 1048576.f && fabsf(b) < 1048576.f;
+  *oor |= !ok;
+  *ff = ok ? (uint32_t)((int)a + 1048576) : 0u;
+  *fr = ok ? (uint32_t)((int)b + 1048576) : 0u;
+  return false;
+}
+
+// sum over the three fields of (2^21 + 1) * 2^(21 i): KEY_MIRROR - key mirrors every field
+constexpr uint64_t KEY_MIRROR = 2097153ull * ((1ull << 42) + (1ull << 21) + 1ull);
+
+// Keys of row (m, n) and, ordered, of row (n, m) from the baseline diffs d.
+__device__ __forceinline__ void row_keys(const float* d, double lambda, float scale32, int ordered, uint64_t* kf,
+                                         uint64_t* kr, bool* oor) {
+  uint32_t ff[3], fr[3];
+  bool fc[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) fc[c] = coord_fields(d[c], lambda, scale32, &ff[c], &fr[c], oor);
+  *kf = ((uint64_t)ff[0] << 42) | ((uint64_t)ff[1] << 21) | (uint64_t)ff[2];
+  if (!ordered) return;
+  if (fc[0] && fc[1] && fc[2]) {
+    *kr = KEY_MIRROR - *kf;
+    return;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)  // fields of the slow coordinates are exact already
+    if (fc[c]) fr[c] = 2097153u - ff[c];
+  *kr = ((uint64_t)fr[0] << 42) | ((uint64_t)fr[1] << 21) | (uint64_t)fr[2];
+}
+
+__global__ void __launch_bounds__(256, 6) unique_insert_kernel(const float* __restrict__ pos, int64_t S, int nsat,
+                                                            int ordered, int npairs, double lambda, float scale32,
+                                                            uint64_t* tkeys, uint32_t* tidx, uint64_t mask, int* bad,
+                                                            int* overflow) {
+  const int nup = nsat * (nsat - 1) / 2;  // satellite pairs m < n
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t chunk = t / nup;
+  const int up = (int)(t - chunk * nup);
+  const int64_t g0 = chunk * UNIQUE_RUN;
+  if (g0 >= S) return;
+  const int cnt = (int)(g0 + UNIQUE_RUN < S ? UNIQUE_RUN : S - g0);
+  int m, n;
+  pair_of(up, nsat, 0, &m, &n);
+  // row offsets within a snapshot: (m, n) and, ordered, (n, m) (pair_of's order)
+  const int qf = ordered ? m * (nsat - 1) + (n - 1) : up;
+  const int qr = n * (nsat - 1) + m;
+  const int stride = nsat * 3;
+  const float* pm = pos + (g0 * nsat + m) * 3;
+  const float* pn = pos + (g0 * nsat + n) * 3;
+  const float* pend = pos + (g0 + cnt) * nsat * 3;  // prefetches stay inside the chunk
+  // keys of the snapshot before the chunk: a row equal to it is no first occurrence
+  uint64_t prevf = DEDUP_EMPTY, prevr = DEDUP_EMPTY;  // no key equals it (bit 63 is never set)
+  bool oor = false;
+  if (g0 > 0) {
+    const float dp[3] = {__ldg(pn - stride) - __ldg(pm - stride), __ldg(pn - stride + 1) - __ldg(pm - stride + 1),
+                         __ldg(pn - stride + 2) - __ldg(pm - stride + 2)};
+    row_keys(dp, lambda, scale32, ordered, &prevf, &prevr, &oor);
+  }
+  uint32_t rowf = (uint32_t)(qf * S + g0), rowr = (uint32_t)(qr * S + g0);
+  for (int j0 = 0; j0 < cnt; j0 += 4) {
+    const float* ahead = pn + (j0 + 32) * stride;
+    if (ahead < pend) asm volatile("prefetch.global.L2 [%0];" ::"l"(ahead));
+    float d[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int o = (j0 + j < cnt ? j0 + j : cnt - 1) * stride;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) d[j][c] = __ldg(pn + o + c) - __ldg(pm + o + c);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (j0 + j >= cnt) break;
+      uint64_t kf, kr;
+      row_keys(d[j], lambda, scale32, ordered, &kf, &kr, &oor);
+      if (kf != prevf) dedup_insert(tkeys, tidx, mask, kf, rowf, overflow);
+      prevf = kf;
+      ++rowf;
+      if (ordered) {
+        if (kr != prevr) dedup_insert(tkeys, tidx, mask, kr, rowr, overflow);
+        prevr = kr;
+        ++rowr;
+      }
+    }
+  }
+  if (oor) atomicOr(bad, 1);
+}
+
+// occupied slots -> (key, first row) pairs, in any order (they are sorted next).
+// A block takes COMPACT_SLOTS slots and one atomic on the counter.
+constexpr int COMPACT_PER_THREAD = 16;
+constexpr int COMPACT_SLOTS = 256 * COMPACT_PER_THREAD;
+
+__global__ void __launch_bounds__(256) unique_compact_kernel(const uint64_t* tkeys, const uint32_t* tidx, int64_t T,
+                                                             uint64_t* k1, uint32_t* i1,
+                                                             unsigned long long* count) {
+  __shared__ unsigned warp_sum[8];
+  __shared__ unsigned long long block_base;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int64_t base = (int64_t)blockIdx.x * COMPACT_SLOTS + tid;
+  uint64_t keys[COMPACT_PER_THREAD];
+  unsigned mine = 0;
+#pragma unroll
+  for (int i = 0; i < COMPACT_PER_THREAD; ++i) {
+    const int64_t sl = base + (int64_t)i * 256;
+    keys[i] = sl < T ? tkeys[sl] : DEDUP_EMPTY;
+    mine += keys[i] != DEDUP_EMPTY;
+  }
+  unsigned incl = mine;  // inclusive warp scan
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) warp_sum[wid] = incl;
+  __syncthreads();
+  unsigned before = 0, total = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) {
+    before += w < wid ? warp_sum[w] : 0;
+    total += warp_sum[w];
+  }
+  if (tid == 0) block_base = total ? atomicAdd(count, (unsigned long long)total) : 0ull;
+  __syncthreads();
+  unsigned long long at = block_base + before + incl - mine;
+#pragma unroll
+  for (int i = 0; i < COMPACT_PER_THREAD; ++i) {
+    if (keys[i] != DEDUP_EMPTY) {
+      k1[at] = keys[i];
+      i1[at] = tidx[base + (int64_t)i * 256];
+      ++at;
+    }
+  }
+}
+
+// sorted unique row indices -> their uvw, recomputed as the baselines kernel does
+__global__ void unique_emit_kernel(const uint32_t* idx, const int64_t* n, const float* pos, int64_t S, int nsat,
+                                   int ordered, double lambda, float scale32, float* u, float* v, float* w) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *n) return;
+  const int64_t r = idx[k];  // pair-major row q * S + g
+  const int64_t q = r / S;
+  const int64_t g = r - q * S;
+  int m, nn;
+  pair_of((int)q, nsat, ordered, &m, &nn);
+  const float* pm = pos + (g * nsat + m) * 3;
+  const float* pn = pos + (g * nsat + nn) * 3;
+  u[k] = baseline_coord(pn[0] - pm[0], lambda, scale32, 1);
+  v[k] = baseline_coord(pn[1] - pm[1], lambda, scale32, 1);
+  w[k] = baseline_coord(pn[2] - pm[2], lambda, scale32, 1);
+}
+
 __global__ void dedup_table_init_kernel(uint64_t* tkeys, uint32_t* tidx, int64_t n) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) { tkeys[t] = DEDUP_EMPTY; tidx[t] = 0xffffffffu; }
-}
-
-__global__ void dedup_occupied_kernel(const uint64_t* tkeys, int64_t n, int* flag) {
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < n) flag[t] = tkeys[t] != DEDUP_EMPTY;
 }
 
 // sorted unique rows -> u, v, w (the first occurrence's values)
@@ -296,14 +574,32 @@ struct DedupPlan {
                                     (uint32_t*)nullptr, (int64_t)K, 0, 63);
     cub::DeviceSelect::Flagged(nullptr, b, (float*)nullptr, (int*)nullptr, (float*)nullptr, (int64_t*)nullptr,
                                (int64_t)K);
-    size_t c2 = 0, c3 = 0;
-    cub::DeviceSelect::Flagged(nullptr, c2, (uint64_t*)nullptr, (int*)nullptr, (uint64_t*)nullptr,
-                               (int64_t*)nullptr, (int64_t)K);
-    cub::DeviceSelect::Flagged(nullptr, c3, (uint32_t*)nullptr, (int*)nullptr, (uint32_t*)nullptr,
-                               (int64_t*)nullptr, (int64_t)K);
     cub_bytes = a > b ? a : b;
-    if (c2 > cub_bytes) cub_bytes = c2;
-    if (c3 > cub_bytes) cub_bytes = c3;
+    cub = c.take<char>(cub_bytes);
+    bytes = c.size();
+  }
+};
+
+// Workspace of viss_unique_uvw: a table of up to T = 2K slots (pow2, 2^10 ..
+// 2^28), the compacted (key, first row) pairs and the CUB scratch.
+struct UniquePlan {
+  int64_t T = 0;
+  uint64_t *tkeys = nullptr, *k1 = nullptr;
+  uint32_t *tidx = nullptr, *i1 = nullptr;
+  int* bad = nullptr;
+  int64_t* nsel = nullptr;
+  void* cub = nullptr;
+  size_t cub_bytes = 0, bytes = 0;
+  void layout(void* ws, int64_t K) {
+    T = 1024;
+    while (T < 2 * K && T < ((int64_t)1 << 28)) T <<= 1;
+    Carver c(ws);
+    tkeys = c.take<uint64_t>(T); k1 = c.take<uint64_t>(T);
+    tidx = c.take<uint32_t>(T); i1 = c.take<uint32_t>(T);
+    bad = c.take<int>(4);
+    nsel = c.take<int64_t>(4);
+    cub::DeviceRadixSort::SortPairs(nullptr, cub_bytes, (uint64_t*)nullptr, (uint64_t*)nullptr, (uint32_t*)nullptr,
+                                    (uint32_t*)nullptr, T, 0, 63);
     cub = c.take<char>(cub_bytes);
     bytes = c.size();
   }
@@ -334,8 +630,17 @@ int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, v
   o.interval = cfg->orbit_res / 360 * 10;
   o.total = (int64_t)cfg->orbit_res * cfg->orbit_counts;
   o.S = (int64_t)cfg->orbit_counts * o.span;
+  o.half = o.total / 2;
+  o.reset_index = o.total / (o.orbit_res + o.interval) + 1;
+  o.by_span.set(o.span);
+  o.by_res.set(o.orbit_res);
+  o.by_nsat.set(o.nsat);
   o.d2r = (float)(kPi / 180);
   o.a = (float)cfg->a_km; o.e = (float)cfg->e;
+  o.dm_den = (double)(2.0f * o.a) * 1e3;  // exact: 24-bit x 10-bit
+  o.dm_hi = (float)o.dm_den;
+  o.dm_lo = (float)(o.dm_den - (double)o.dm_hi);
+  o.dm_inv = (float)(1.0 / o.dm_den);
   o.incl = (float)cfg->incl_deg * o.d2r;
   o.argp = (float)cfg->argp_deg * o.d2r;
   o.a64 = cfg->a_km; o.e64 = cfg->e; o.incl64 = cfg->incl_deg * kPi / 180.0; o.argp64 = cfg->argp_deg * kPi / 180.0;
@@ -413,17 +718,15 @@ int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, 
     VISS_CUDA(cudaStreamSynchronize(st));
     if (hb[0]) return fail(VISS_ERR_RANGE, "dedup needs integer-valued uvw with |x| < 2^20");
     if (!hb[1]) {
-      dedup_occupied_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(p.k0, T, p.flag);
-      VISS_LAUNCH_CHECK("dedup_occupied_kernel");
-      size_t cb = p.cub_bytes;
-      VISS_CUDA(cub::DeviceSelect::Flagged(p.cub, cb, p.k0, p.flag, p.k1, p.nsel, T, st));
-      cb = p.cub_bytes;
-      VISS_CUDA(cub::DeviceSelect::Flagged(p.cub, cb, p.i0, p.flag, p.i1, p.nsel, T, st));
+      VISS_CUDA(cudaMemsetAsync(p.nsel, 0, sizeof(int64_t), st));
+      unique_compact_kernel<<<(unsigned)((T + COMPACT_SLOTS - 1) / COMPACT_SLOTS), 256, 0, st>>>(
+          p.k0, p.i0, T, p.k1, p.i1, (unsigned long long*)p.nsel);
+      VISS_LAUNCH_CHECK("unique_compact_kernel");
       int64_t n = 0;
       VISS_CUDA(cudaMemcpyAsync(&n, p.nsel, sizeof(n), cudaMemcpyDeviceToHost, st));
       VISS_CUDA(cudaStreamSynchronize(st));
       // unique keys: the sort's stability does not matter
-      cb = p.cub_bytes;
+      size_t cb = p.cub_bytes;
       VISS_CUDA(cub::DeviceRadixSort::SortPairs(p.cub, cb, p.k1, p.k0, p.i1, p.i0, n, 0, 63, st));
       if (n > 0) {
         dedup_emit_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p.i0, p.nsel, u, v, w, p.tu, p.tv, p.tw);
@@ -459,6 +762,74 @@ int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, 
   VISS_CUDA(cudaStreamSynchronize(st));
   if (bad) return fail(VISS_ERR_RANGE, "dedup needs integer-valued uvw with |x| < 2^20");
   *count_out = cnt;
+  return VISS_OK;
+}
+
+size_t viss_unique_uvw_workspace(int64_t S, int32_t nsat, int ordered) {
+  if (S <= 0 || nsat < 2 || nsat > 32) return 0;
+  UniquePlan p;
+  p.layout(nullptr, S * (ordered ? nsat * (nsat - 1) : nsat * (nsat - 1) / 2));
+  return p.bytes;
+}
+
+int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int ordered, double lambda_m, float* u, float* v,
+                    float* w, int64_t capacity, int64_t* count_out, void* workspace, size_t workspace_bytes,
+                    void* stream) {
+  if (!count_out) return fail(VISS_ERR_INVALID, "count_out NULL");
+  *count_out = 0;
+  if (nsat < 2 || nsat > 32) return fail(VISS_ERR_RANGE, "nsat must be in [2, 32]");
+  if (!(lambda_m > 0)) return fail(VISS_ERR_RANGE, "lambda must be > 0");
+  if (S < 0 || capacity < 0) return fail(VISS_ERR_RANGE, "S < 0 or capacity < 0");
+  if (S == 0) return VISS_OK;
+  if (!pos) return fail(VISS_ERR_INVALID, "pos NULL");
+  if (capacity > 0 && (!u || !v || !w)) return fail(VISS_ERR_INVALID, "u/v/w NULL");
+  const int npairs = ordered ? nsat * (nsat - 1) : nsat * (nsat - 1) / 2;
+  const int64_t K = S * npairs;
+  if (K >= ((int64_t)1 << 32)) return fail(VISS_ERR_RANGE, "S x pairs must be < 2^32");
+  UniquePlan p;
+  p.layout(nullptr, K);
+  if (!workspace || workspace_bytes < p.bytes) return fail(VISS_ERR_WORKSPACE, "unique_uvw workspace too small");
+  if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(VISS_ERR_WORKSPACE, "workspace misaligned");
+  p.layout(workspace, K);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const float scale32 = (float)(1e3 / lambda_m);
+  const int64_t threads = (S + UNIQUE_RUN - 1) / UNIQUE_RUN * (nsat * (nsat - 1) / 2);
+  // a table of 2^25 slots first (the few tens of millions of unique rows of an
+  // orbit campaign), the workspace's full table if that one fills
+  int64_t n = 0;
+  for (int64_t T = p.T < ((int64_t)1 << 25) ? p.T : ((int64_t)1 << 25);; T = p.T) {
+    VISS_CUDA(cudaMemsetAsync(p.bad, 0, 4 * sizeof(int), st));
+    VISS_CUDA(cudaMemsetAsync(p.nsel, 0, sizeof(int64_t), st));
+    dedup_table_init_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(p.tkeys, p.tidx, T);
+    VISS_LAUNCH_CHECK("dedup_table_init_kernel");
+    unique_insert_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        pos, S, nsat, ordered, npairs, lambda_m, scale32, p.tkeys, p.tidx, (uint64_t)(T - 1), p.bad, p.bad + 1);
+    VISS_LAUNCH_CHECK("unique_insert_kernel");
+    unique_compact_kernel<<<(unsigned)((T + COMPACT_SLOTS - 1) / COMPACT_SLOTS), 256, 0, st>>>(
+        p.tkeys, p.tidx, T, p.k1, p.i1, (unsigned long long*)p.nsel);
+    VISS_LAUNCH_CHECK("unique_compact_kernel");
+    int hb[2] = {0, 0};
+    VISS_CUDA(cudaMemcpyAsync(hb, p.bad, sizeof(hb), cudaMemcpyDeviceToHost, st));
+    VISS_CUDA(cudaMemcpyAsync(&n, p.nsel, sizeof(n), cudaMemcpyDeviceToHost, st));
+    VISS_CUDA(cudaStreamSynchronize(st));
+    if (hb[0]) return fail(VISS_ERR_RANGE, "uvw beyond |x| < 2^20 cannot be keyed");
+    if (!hb[1]) break;
+    if (T == p.T)
+      return fail(VISS_ERR_RANGE, "more unique uvw than the table holds: use viss_baseline_uvw + viss_dedup_uvw");
+  }
+  *count_out = n;
+  if (n > capacity) {
+    if (capacity == 0) return VISS_OK;  // count only
+    return fail(VISS_ERR_RANGE, "capacity below the unique count (in *count_out)");
+  }
+  // unique keys, sorted with their first rows back into the table's buffers
+  size_t cb = p.cub_bytes;
+  VISS_CUDA(cub::DeviceRadixSort::SortPairs(p.cub, cb, p.k1, p.tkeys, p.i1, p.tidx, n, 0, 63, st));
+  if (n > 0) {
+    unique_emit_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p.tidx, p.nsel, pos, S, nsat, ordered,
+                                                                    lambda_m, scale32, u, v, w);
+    VISS_LAUNCH_CHECK("unique_emit_kernel");
+  }
   return VISS_OK;
 }
 
