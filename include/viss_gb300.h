@@ -198,6 +198,12 @@ VISS_API int viss_nxq(const float* NX, int64_t X, int64_t J, int32_t* countLoc, 
  * the reference's form, 8 = a fine-map index outside [0, X) (that pixel is NaN).
  * No counterpart in the reference, which reads such inputs unchecked. */
 VISS_API int viss_workspace_flags(const void* workspace, int32_t* flags, void* stream);
+/* GEOMETRIC mask: how many occlusion tests of the completed pass fell within 2e-6 (in the
+ * cosine of the angle to the limb) of the Moon's limb and were decided in double from the
+ * original inputs instead (count of (visibility, pixel, satellite) tests; the fast kernels
+ * test fewer terms than the plain ones, as they drop blocks the cones decide).  Reads the
+ * workspace like viss_workspace_flags (synchronises `stream`). */
+VISS_API int viss_workspace_limb_count(const void* workspace, int64_t* count, void* stream);
 
 /* Batched passes: many frequency channels (or periods) in one persistent
  * launch.  The reference runs one channel per program run or per OpenMP

@@ -368,7 +368,7 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
       viss_sky sc = sky;
       if (bt.bright) sc.bright = bt.bright + (int64_t)c * sky.J;
       if ((rc = launch_vis_plain(cfg, sc, channel_rows(vis, r0, r1), geo, p.satdir, dlmn,
-                                 reinterpret_cast<float2*>(V) + r0, st, map)))
+                                 reinterpret_cast<float2*>(V) + r0, st, map, p.flags)))
         return rc;
     }
     return VISS_OK;
@@ -466,7 +466,7 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
       viss_dft_cfg cc = cfg;
       cc.norm = bt.norm[c];
       if ((rc = launch_recon_plain(cc, sky, vc, geo, V + 2 * r0, ratios, p.satdir, dlmn, F2 + (int64_t)c * sky.J,
-                                   st)))
+                                   st, p.flags)))
         return rc;
     }
     return VISS_OK;
@@ -643,6 +643,15 @@ int viss_workspace_flags(const void* workspace, int32_t* flags, void* stream) {
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the flag words are the first carve of every pass's workspace
   VISS_CUDA(cudaMemcpyAsync(flags, static_cast<const int*>(workspace) + FLAG_ERR, sizeof(int32_t),
+                            cudaMemcpyDeviceToHost, st));
+  VISS_CUDA(cudaStreamSynchronize(st));
+  return VISS_OK;
+}
+
+int viss_workspace_limb_count(const void* workspace, int64_t* count, void* stream) {
+  if (!workspace || !count) return fail(VISS_ERR_INVALID, "workspace or count is NULL");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  VISS_CUDA(cudaMemcpyAsync(count, static_cast<const int*>(workspace) + FLAG_LIMB, sizeof(int64_t),
                             cudaMemcpyDeviceToHost, st));
   VISS_CUDA(cudaStreamSynchronize(st));
   return VISS_OK;

@@ -26,6 +26,7 @@ namespace viss {
 
 // Exact decision near the limb (rare), out of line.
 __device__ __noinline__ bool geo_exact_pix(const ReconParams& p, int j, int gidx) {
+  count_limb(p.flags);
   return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
 }
 
@@ -406,6 +407,7 @@ struct PlainRecArgs {
   float norm;
   double R;
   float2* out;
+  int* flags;  // near-limb count (may be null)
 };
 
 __global__ void recon_plain_kernel(const PlainRecArgs a) {
@@ -423,8 +425,8 @@ __global__ void recon_plain_kernel(const PlainRecArgs a) {
     } else if (a.rmask == VISS_RECON_MASK_GEOMETRIC) {
       const int s = a.snap[k], pr = a.pair[k];
       const int64_t g1 = (int64_t)s * a.nsat + (pr & 0xffff), g2 = (int64_t)s * a.nsat + ((pr >> 16) & 0xffff);
-      if (geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g1], a.sat_pos + 3 * g1, a.R) ||
-          geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g2], a.sat_pos + 3 * g2, a.R))
+      if (geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g1], a.sat_pos + 3 * g1, a.R, a.flags) ||
+          geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g2], a.sat_pos + 3 * g2, a.R, a.flags))
         continue;
     }
     const float ph = a.u[k] * lj / a.dl + a.v[k] * mj / a.dm + a.w[k] * nj / a.dn;
@@ -440,8 +442,9 @@ __global__ void recon_plain_kernel(const PlainRecArgs a) {
 
 int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                        const viss_geometry* geo, const float* V, const float* ratios, const float4* satdir,
-                       const float* dlmn, float2* out, cudaStream_t st) {
+                       const float* dlmn, float2* out, cudaStream_t st, int* flags) {
   PlainRecArgs a{};
+  a.flags = flags;
   a.satdir = satdir;
   a.u = vis.u; a.v = vis.v; a.w = vis.w; a.wgt = vis.wgt; a.V = V;
   a.l = sky.l; a.m = sky.m; a.n = sky.n;

@@ -48,6 +48,7 @@ __device__ __forceinline__ void vis_term(const int4& a, const int4& b, const flo
 // Exact decision near the limb (rare): kept out of line so its double-precision
 // registers do not weigh on the hot loops.
 __device__ __noinline__ bool geo_exact_at(const VisParams& p, int j, int gidx) {
+  count_limb(p.flags);
   return geo_occluded_exact(p.l[j], p.m[j], p.n[j], p.sat_pos + 3 * (int64_t)gidx, p.R);
 }
 
@@ -478,6 +479,7 @@ struct PlainVisArgs {
   float trail;  // 1 + n_offset
   double R;
   float2* out;
+  int* flags;  // near-limb count (may be null)
   // non-identity fine->coarse map: FF, NXq (float or int), countLoc
   const float* FF;
   const float* NXq_f;
@@ -534,14 +536,16 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
     if (a.countLoc) {
       if (geo) {
         const float sx = a.l[j], sy = a.m[j], sz = a.n[j];
-        if (geo_test_plain(sx, sy, sz, d1, p1, a.R) || geo_test_plain(sx, sy, sz, d2, p2, a.R)) c = a.occ;
+        if (geo_test_plain(sx, sy, sz, d1, p1, a.R, a.flags) || geo_test_plain(sx, sy, sz, d2, p2, a.R, a.flags))
+          c = a.occ;
       }
     } else if (wv.x <= wv.y) {
       const int64_t q = j / a.res, r = j % a.res;
       if (ref_hit(wv, (int)q, (int)r, j, a.res)) c = a.occ;
     } else if (geo) {
       const float sx = a.l[j], sy = a.m[j], sz = a.n[j];
-      if (geo_test_plain(sx, sy, sz, d1, p1, a.R) || geo_test_plain(sx, sy, sz, d2, p2, a.R)) c = a.occ;
+      if (geo_test_plain(sx, sy, sz, d1, p1, a.R, a.flags) || geo_test_plain(sx, sy, sz, d2, p2, a.R, a.flags))
+        c = a.occ;
     }
     const float ph = uk * a.l[j] / a.dl + vk * a.m[j] / a.dm + wk * (a.n[j] - 1.0f) / a.dn;
     float sn, cs;
@@ -556,8 +560,9 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
 
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                      const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
-                     const viss_fine_map* map) {
+                     const viss_fine_map* map, int* flags) {
   PlainVisArgs a{};
+  a.flags = flags;
   if (map) {
     a.FF = map->FF; a.NXq_f = map->NXq_f; a.NXq_i = map->NXq_i; a.countLoc = map->countLoc; a.X = map->X;
   }

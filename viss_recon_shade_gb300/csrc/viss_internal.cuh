@@ -200,7 +200,14 @@ struct RowPrepArgs {
 };
 
 // flags words of a pass
-constexpr int FLAG_FRAC = 0, FLAG_ERR = 1, FLAG_VIS_COUNTER = 8, FLAG_REC_COUNTER = 9, FLAG_WORDS = 64;
+// flag words at the start of every pass's workspace; FLAG_LIMB (words 2-3) counts,
+// as one 64-bit integer, the geometric decisions settled in double near the limb
+constexpr int FLAG_FRAC = 0, FLAG_ERR = 1, FLAG_LIMB = 2, FLAG_VIS_COUNTER = 8, FLAG_REC_COUNTER = 9,
+              FLAG_WORDS = 64;
+
+__device__ __forceinline__ void count_limb(int* flags) {
+  if (flags) atomicAdd(reinterpret_cast<unsigned long long*>(flags + FLAG_LIMB), 1ull);
+}
 
 // A fine sky grid mapped onto the coarse pixels: pixel (position) j has
 // members[start_j .. start_j + cnt_j), fine indices as the reference reads them
@@ -328,22 +335,23 @@ int prep_fine_map(const float* NXq_f, const int32_t* NXq_i, const int32_t* count
 int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st);
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                      const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
-                     const viss_fine_map* map = nullptr);
+                     const viss_fine_map* map = nullptr, int* flags = nullptr);
 
 int launch_recon_fast(const ReconParams& p, int ctas_per_sm, bool compensated, cudaStream_t st);
 int launch_recon_reduce(const RecReduceParams& p, cudaStream_t st);
 int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                        const viss_geometry* geo, const float* V, const float* ratios, const float4* satdir,
-                       const float* dlmn, float2* out, cudaStream_t st);
+                       const float* dlmn, float2* out, cudaStream_t st, int* flags = nullptr);
 
 // Fast geometric test of direction s (need not be unit) against satellite
 // direction d = {p_hat, cos alpha}: s_hat.p_hat + cos(alpha) < 0, decided in
 // double (from the original inputs) within GEO_EPS of the limb.
 __device__ __forceinline__ bool geo_test_plain(float sx, float sy, float sz, const float4& d, const float* pos,
-                                               double R) {
+                                               double R, int* flags) {
   const float inv = rsqrtf(fmaf(sx, sx, fmaf(sy, sy, sz * sz)));
   const float e = fmaf(sx * inv, d.x, fmaf(sy * inv, d.y, fmaf(sz * inv, d.z, d.w)));
   if (fabsf(e) >= 4.0f * GEO_EPS) return e < 0.f;
+  count_limb(flags);
   return geo_occluded_exact(sx, sy, sz, pos, R);
 }
 
