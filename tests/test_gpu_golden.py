@@ -73,8 +73,9 @@ def test_visscal_imagerecon_vs_reference_kernels(V, oracle, case, variant, trunc
 @pytest.mark.parametrize("tag", ["a", "b"])
 def test_orbit_uvw_vs_reference_kernels(V, tag):
     """FP32 positions evaluate the reference's formulas with the same CUDA math
-    functions; they match the reference kernels' positions to the last bit for
-    almost every sample, and uvw (ceil) follow."""
+    functions in the same expression shapes; they match the reference kernels'
+    positions to the last bit (all samples of both cases on GB300; the bound
+    leaves room for a rare ulp), and uvw (ceil) follow."""
     z = load("ref_orbit.npz")
     nsat, orbit_res, orbit_counts, index, freq = z[f"{tag}_cfg"]
     cfg = V.OrbitConfig(nsat=int(nsat), orbit_res=int(orbit_res), orbit_counts=int(orbit_counts), index=int(index),
@@ -82,7 +83,7 @@ def test_orbit_uvw_vs_reference_kernels(V, tag):
     pos = V.orbit_positions(cfg).cpu().numpy()
     ref = z[f"{tag}_pos"]
     exact = np.all(pos == ref, axis=2)
-    assert exact.mean() > 0.99, exact.mean()
+    assert exact.mean() >= 0.999, exact.mean()
     assert np.abs(pos - ref).max() / 2038.14 < 2e-6
     u, v, w, snap, pair = V.baseline_uvw(torch.from_numpy(pos).cuda(), float(int(3e8 / freq)), ordered=True,
                                          rounding=True)

@@ -117,7 +117,10 @@ __device__ __noinline__ float raan_of(int k, int base, float d2r, double step) {
 constexpr int RAAN_TAB = 4;  // orbits per block with a precomputed RAAN
 
 // calculateOrbit (:83-110) in the reference's arithmetic.  raan_tab holds the
-// RAAN of orbits k_base .. k_base + RAAN_TAB - 1.
+// RAAN of orbits k_base .. k_base + RAAN_TAB - 1.  The final rotation keeps the
+// reference's expression shape: written with cosf/sinf values computed elsewhere
+// the compiler fuses its products differently, and about half of the positions
+// move by an ulp.
 __device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const float* raan_tab, int k_base,
                              float* out) {
   const int64_t half = o.half;
@@ -252,6 +255,7 @@ __device__ __noinline__ float ceil_quotient_exact(float diff, double lambda) {
 // Elsewhere, and for |x| >= 2^22 where x - floor(x) stops being exact, the
 // quotient is taken in double.
 __device__ __forceinline__ float baseline_coord(float diff, double lambda, float scale32, int rounding) {
+  if (diff == 0.f) return diff;  // +-0 * 1e3 / lambda and its ceil keep the sign of zero
   if (!rounding) return (float)((double)diff * 1e3 / lambda);
   const float x = diff * scale32;
   const float f = x - floorf(x);
@@ -374,10 +378,15 @@ constexpr int UNIQUE_RUN = 256;
 // where the fast-path test of baseline_coord holds (for -x exactly when for x),
 // and ceil(-x) = -floor(x): F(n, m) = 2^21 + 1 - F(m, n).  With |x| < 2^20 - 2 as
 // well, both fields lie in [2, 2^21 - 2] and the three fields of (n, m) are one
-// 64-bit subtraction from those of (m, n).  Returns false where the slow path
-// decides (fields then exact, or 0 with *oor set when out of |c| < 2^20).
+// 64-bit subtraction from those of (m, n).  Returns false where the fields are
+// set otherwise: diff = 0 (both 0), or the slow path (exact, or 0 with *oor set
+// when out of |c| < 2^20).
 __device__ __forceinline__ bool coord_fields(float diff, double lambda, float scale32, uint32_t* ff, uint32_t* fr,
                                              bool* oor) {
+  if (diff == 0.f) {  // equal positions (the reference's zero-filled samples): 0 both ways
+    *ff = *fr = 1048576u;
+    return false;
+  }
   const float x = diff * scale32;
   const float y = __fadd_rd(x, 12582912.f);
   const float f = x - (y - 12582912.f);
