@@ -247,24 +247,40 @@ __device__ __noinline__ float ceil_quotient_exact(float diff, double lambda) {
   return (float)ceil((double)diff * 1e3 / lambda);
 }
 
-// computeUVW (:156-158) for one coordinate of a float baseline diff = x_n - x_m:
-// ceil((double)diff * 1e3 / lambda) as float, or without the ceil.  The FP32
-// product x = diff * fl(1e3 / lambda) is within 2^-23 |x| of the quotient; where
-// x lies more than 2^-21 |x| inside (n, n + 1) the quotient and its double
-// rounding do too, so ceilf(x) is the same integer (and sign of zero).
-// Elsewhere, and for |x| >= 2^22 where x - floor(x) stops being exact, the
-// quotient is taken in double.
-__device__ __forceinline__ float baseline_coord(float diff, double lambda, float scale32, int rounding) {
+// The reference's ceil((double)diff * 1e3 / lambda) (computeUVW, :156-158) from
+// FP32 arithmetic where that is certain.  scale = {hi, lo} holds 1e3 / lambda to
+// 2^-48; x = diff * scale is carried as xh + xl to 2^-45 |x| (xh rounded, xl its
+// FMA residual plus diff * lo).  floor(xh) comes from the round-down sum
+// xh + 1.5 * 2^23 (exact for |xh| < 2^22), and f2 = (xh - floor(xh)) + xl is the
+// quotient's distance above that integer to within 2^-24 + 2^-45 |x|.  Where f2
+// keeps T = 2^-23 + 2^-44 |x| from both ends, the quotient and its double
+// rounding lie strictly inside (floor, floor + 1): the ceil is floor + 1, the
+// floor of the negated quotient -(floor + 1) + 1.  Elsewhere (a few in 10^7 for
+// orbit baselines, and |x| >= 2^22) the quotient is taken in double.
+// Returns whether the fast path holds; *y = floor(xh) + 1.5 * 2^23.
+__device__ __forceinline__ bool ceil_is_floor_plus_one(float diff, float2 scale, float* y) {
+  const float xh = __fmul_rn(diff, scale.x);
+  const float xl = __fmaf_rn(diff, scale.y, __fmaf_rn(diff, scale.x, -xh));
+  const float yy = __fadd_rd(xh, 12582912.f);
+  const float f2 = __fadd_rn(__fsub_rn(xh, __fsub_rn(yy, 12582912.f)), xl);
+  const float T = __fmaf_rn(fabsf(xh), 0x1p-44f, 0x1p-23f);
+  *y = yy;
+  return fabsf(xh) < 4194304.f && f2 > T && f2 < 1.f - T;
+}
+
+// computeUVW (:156-158) for one coordinate: ceil((double)diff * 1e3 / lambda) as
+// float (the sign of zero included: (-1, 0) gives -0), or without the ceil.
+__device__ __forceinline__ float baseline_coord(float diff, double lambda, float2 scale, int rounding) {
   if (diff == 0.f) return diff;  // +-0 * 1e3 / lambda and its ceil keep the sign of zero
   if (!rounding) return (float)((double)diff * 1e3 / lambda);
-  const float x = diff * scale32;
-  const float f = x - floorf(x);
-  const float tol = fabsf(x) * 4.76837158203125e-7f + 1e-30f;
-  return (fabsf(x) < 4194304.f && f > tol && 1.f - f > tol) ? ceilf(x) : ceil_quotient_exact(diff, lambda);
+  float y;
+  // floor + 1 rounded down: an exact sum, -0 for floor = -1 as ceil gives
+  if (ceil_is_floor_plus_one(diff, scale, &y)) return __fadd_rd(__fsub_rn(y, 12582912.f), 1.f);
+  return ceil_quotient_exact(diff, lambda);
 }
 
 __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64_t S, int nsat, int ordered, int npairs,
-                                    uint64_t pair_magic, double lambda, float scale32, int rounding, float* u,
+                                    uint64_t pair_magic, double lambda, float2 scale, int rounding, float* u,
                                     float* v, float* w, int32_t* snap, int32_t* pair) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= S * npairs) return;
@@ -282,7 +298,7 @@ __global__ void baseline_uvw_kernel(const float* pos, const double* pos64, int64
       out[c] = rounding ? (float)ceil(x) : (float)x;
       continue;
     }
-    out[c] = baseline_coord(pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c], lambda, scale32, rounding);
+    out[c] = baseline_coord(pos[(g * nsat + n) * 3 + c] - pos[(g * nsat + m) * 3 + c], lambda, scale, rounding);
   }
   u[k] = out[0]; v[k] = out[1]; w[k] = out[2];
   if (snap) snap[k] = (int32_t)g;
@@ -353,6 +369,26 @@ __device__ __forceinline__ void dedup_insert(uint64_t* tkeys, uint32_t* tidx, ui
   atomicOr(overflow, 1);
 }
 
+// The same for rows that mostly bring a new key or one last seen long ago (the
+// fused pass): the row index is lowered by a reduction that does not wait for
+// its result, one dependent trip fewer per insert.
+__device__ __forceinline__ void dedup_insert_red(uint64_t* tkeys, uint32_t* tidx, uint64_t mask, uint64_t key,
+                                                 uint32_t k, int* overflow) {
+  uint64_t h = dedup_hash(key) & mask;
+  for (int probe = 0; probe < DEDUP_PROBES; ++probe, h = (h + 1) & mask) {
+    uint64_t cur = *((volatile uint64_t*)(tkeys + h));
+    if (cur == DEDUP_EMPTY) {
+      cur = atomicCAS((unsigned long long*)(tkeys + h), (unsigned long long)DEDUP_EMPTY, (unsigned long long)key);
+      if (cur == DEDUP_EMPTY) cur = key;
+    }
+    if (cur == key) {
+      atomicMin(tidx + h, k);
+      return;
+    }
+  }
+  atomicOr(overflow, 1);
+}
+
 __global__ void dedup_hash_kernel(const float* u, const float* v, const float* w, int64_t K, uint64_t* tkeys,
                                   uint32_t* tidx, uint64_t mask, int* bad, int* overflow) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -364,35 +400,29 @@ __global__ void dedup_hash_kernel(const float* u, const float* v, const float* w
 // positions [S][nsat][3], ranked pair-major (row q * S + g) as the reference
 // concatenates its per-pair lists before the global sort + unique
 // (MIncline_generate_uvw_float.cu:370-397): the first occurrence of a key is its
-// lowest pair, then its earliest snapshot.  A thread walks one satellite pair m < n over UNIQUE_RUN
-// consecutive snapshots, for ordered pairs both rows (m, n) and (n, m), and
-// inserts a row only where its key differs from the previous snapshot's: an
+// lowest pair, then its earliest snapshot.  A thread walks one satellite pair
+// m < n over consecutive snapshots, for ordered pairs both rows (m, n) and (n, m),
+// and inserts a row only where its key differs from the previous snapshot's: an
 // equal key there has the smaller row index already.  Baselines move by far
 // less than a wavelength between snapshots, so most rows touch no table slot.
 constexpr int UNIQUE_RUN = 256;
 
 // Key fields of row (m, n) and row (n, m) for one coordinate: F = ceil(q) + 2^20
 // with q = (double)(+-diff) * 1e3 / lambda, the integers baseline_coord gives
-// (without their sign of zero).  floor(x) of x = diff * scale32 comes from the
-// round-down sum x + 1.5 * 2^23 (exact for |x| < 2^22), so ceil(x) = floor(x) + 1
-// where the fast-path test of baseline_coord holds (for -x exactly when for x),
-// and ceil(-x) = -floor(x): F(n, m) = 2^21 + 1 - F(m, n).  With |x| < 2^20 - 2 as
-// well, both fields lie in [2, 2^21 - 2] and the three fields of (n, m) are one
-// 64-bit subtraction from those of (m, n).  Returns false where the fields are
-// set otherwise: diff = 0 (both 0), or the slow path (exact, or 0 with *oor set
-// when out of |c| < 2^20).
-__device__ __forceinline__ bool coord_fields(float diff, double lambda, float scale32, uint32_t* ff, uint32_t* fr,
+// (without their sign of zero).  Where ceil(q) = floor + 1 is certain,
+// ceil(-q) = -floor: F(n, m) = 2^21 + 1 - F(m, n).  With |x| < 2^20 - 2 as well,
+// both fields lie in [2, 2^21 - 2] and the three fields of (n, m) are one 64-bit
+// subtraction from those of (m, n).  Returns false where the fields are set
+// otherwise: diff = 0 (both 0), or the slow path (exact, or 0 with *oor set when
+// out of |c| < 2^20).
+__device__ __forceinline__ bool coord_fields(float diff, double lambda, float2 scale, uint32_t* ff, uint32_t* fr,
                                              bool* oor) {
   if (diff == 0.f) {  // equal positions (the reference's zero-filled samples): 0 both ways
     *ff = *fr = 1048576u;
     return false;
   }
-  const float x = diff * scale32;
-  const float y = __fadd_rd(x, 12582912.f);
-  const float f = x - (y - 12582912.f);
-  const float ax = fabsf(x);
-  const float tol = ax * 4.76837158203125e-7f + 1e-30f;
-  if (ax < 1048574.f && f > tol && 1.f - f > tol) {
+  float y;
+  if (ceil_is_floor_plus_one(diff, scale, &y) && fabsf(y - 12582912.f) < 1048573.f) {
     *ff = (uint32_t)(__float_as_int(y) - 0x4b400000 + 1 + 1048576);
     return true;
   }
@@ -408,12 +438,12 @@ __device__ __forceinline__ bool coord_fields(float diff, double lambda, float sc
 constexpr uint64_t KEY_MIRROR = 2097153ull * ((1ull << 42) + (1ull << 21) + 1ull);
 
 // Keys of row (m, n) and, ordered, of row (n, m) from the baseline diffs d.
-__device__ __forceinline__ void row_keys(const float* d, double lambda, float scale32, int ordered, uint64_t* kf,
+__device__ __forceinline__ void row_keys(const float* d, double lambda, float2 scale, int ordered, uint64_t* kf,
                                          uint64_t* kr, bool* oor) {
   uint32_t ff[3], fr[3];
   bool fc[3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) fc[c] = coord_fields(d[c], lambda, scale32, &ff[c], &fr[c], oor);
+  for (int c = 0; c < 3; ++c) fc[c] = coord_fields(d[c], lambda, scale, &ff[c], &fr[c], oor);
   *kf = ((uint64_t)ff[0] << 42) | ((uint64_t)ff[1] << 21) | (uint64_t)ff[2];
   if (!ordered) return;
   if (fc[0] && fc[1] && fc[2]) {
@@ -427,7 +457,7 @@ __device__ __forceinline__ void row_keys(const float* d, double lambda, float sc
 }
 
 __global__ void __launch_bounds__(256, 6) unique_insert_kernel(const float* __restrict__ pos, int64_t S, int nsat,
-                                                            int ordered, int npairs, double lambda, float scale32,
+                                                            int ordered, int npairs, double lambda, float2 scale,
                                                             uint64_t* tkeys, uint32_t* tidx, uint64_t mask, int* bad,
                                                             int* overflow) {
   const int nup = nsat * (nsat - 1) / 2;  // satellite pairs m < n
@@ -452,7 +482,7 @@ __global__ void __launch_bounds__(256, 6) unique_insert_kernel(const float* __re
   if (g0 > 0) {
     const float dp[3] = {__ldg(pn - stride) - __ldg(pm - stride), __ldg(pn - stride + 1) - __ldg(pm - stride + 1),
                          __ldg(pn - stride + 2) - __ldg(pm - stride + 2)};
-    row_keys(dp, lambda, scale32, ordered, &prevf, &prevr, &oor);
+    row_keys(dp, lambda, scale, ordered, &prevf, &prevr, &oor);
   }
   uint32_t rowf = (uint32_t)(qf * S + g0), rowr = (uint32_t)(qr * S + g0);
   for (int j0 = 0; j0 < cnt; j0 += 4) {
@@ -469,12 +499,12 @@ __global__ void __launch_bounds__(256, 6) unique_insert_kernel(const float* __re
     for (int j = 0; j < 4; ++j) {
       if (j0 + j >= cnt) break;
       uint64_t kf, kr;
-      row_keys(d[j], lambda, scale32, ordered, &kf, &kr, &oor);
-      if (kf != prevf) dedup_insert(tkeys, tidx, mask, kf, rowf, overflow);
+      row_keys(d[j], lambda, scale, ordered, &kf, &kr, &oor);
+      if (kf != prevf) dedup_insert_red(tkeys, tidx, mask, kf, rowf, overflow);
       prevf = kf;
       ++rowf;
       if (ordered) {
-        if (kr != prevr) dedup_insert(tkeys, tidx, mask, kr, rowr, overflow);
+        if (kr != prevr) dedup_insert_red(tkeys, tidx, mask, kr, rowr, overflow);
         prevr = kr;
         ++rowr;
       }
@@ -532,7 +562,7 @@ __global__ void __launch_bounds__(256) unique_compact_kernel(const uint64_t* tke
 
 // sorted unique row indices -> their uvw, recomputed as the baselines kernel does
 __global__ void unique_emit_kernel(const uint32_t* idx, const int64_t* n, const float* pos, int64_t S, int nsat,
-                                   int ordered, double lambda, float scale32, float* u, float* v, float* w) {
+                                   int ordered, double lambda, float2 scale, float* u, float* v, float* w) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= *n) return;
   const int64_t r = idx[k];  // pair-major row q * S + g
@@ -542,9 +572,9 @@ __global__ void unique_emit_kernel(const uint32_t* idx, const int64_t* n, const 
   pair_of((int)q, nsat, ordered, &m, &nn);
   const float* pm = pos + (g * nsat + m) * 3;
   const float* pn = pos + (g * nsat + nn) * 3;
-  u[k] = baseline_coord(pn[0] - pm[0], lambda, scale32, 1);
-  v[k] = baseline_coord(pn[1] - pm[1], lambda, scale32, 1);
-  w[k] = baseline_coord(pn[2] - pm[2], lambda, scale32, 1);
+  u[k] = baseline_coord(pn[0] - pm[0], lambda, scale, 1);
+  v[k] = baseline_coord(pn[1] - pm[1], lambda, scale, 1);
+  w[k] = baseline_coord(pn[2] - pm[2], lambda, scale, 1);
 }
 
 __global__ void dedup_table_init_kernel(uint64_t* tkeys, uint32_t* tidx, int64_t n) {
@@ -588,6 +618,13 @@ struct DedupPlan {
     bytes = c.size();
   }
 };
+
+// 1e3 / lambda as a float pair hi + lo (to 2^-48)
+inline float2 scale_pair(double lambda) {
+  const double s = 1e3 / lambda;
+  const float hi = (float)s;
+  return make_float2(hi, (float)(s - (double)hi));
+}
 
 // Workspace of viss_unique_uvw: a table of up to T = 2K slots (pow2, 2^10 ..
 // 2^28), the compacted (key, first row) pairs and the CUB scratch.
@@ -684,7 +721,7 @@ int viss_baseline_uvw(const float* pos, const double* pos64, int64_t S, int32_t 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const uint64_t magic = ~0ull / (uint64_t)npairs + 1;
   baseline_uvw_kernel<<<(unsigned)((K + 255) / 256), 256, 0, st>>>(
-      pos, pos64, S, nsat, ordered, npairs, magic, lambda_m, (float)(1e3 / lambda_m), rounding, u, v, w, snap, pair);
+      pos, pos64, S, nsat, ordered, npairs, magic, lambda_m, scale_pair(lambda_m), rounding, u, v, w, snap, pair);
   VISS_LAUNCH_CHECK("baseline_uvw_kernel");
   return VISS_OK;
 }
@@ -801,7 +838,7 @@ int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int ordered, doub
   if (reinterpret_cast<uintptr_t>(workspace) & 255) return fail(VISS_ERR_WORKSPACE, "workspace misaligned");
   p.layout(workspace, K);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  const float scale32 = (float)(1e3 / lambda_m);
+  const float2 scale = scale_pair(lambda_m);
   const int64_t threads = (S + UNIQUE_RUN - 1) / UNIQUE_RUN * (nsat * (nsat - 1) / 2);
   // a table of 2^25 slots first (the few tens of millions of unique rows of an
   // orbit campaign), the workspace's full table if that one fills
@@ -812,7 +849,7 @@ int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int ordered, doub
     dedup_table_init_kernel<<<(unsigned)((T + 255) / 256), 256, 0, st>>>(p.tkeys, p.tidx, T);
     VISS_LAUNCH_CHECK("dedup_table_init_kernel");
     unique_insert_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
-        pos, S, nsat, ordered, npairs, lambda_m, scale32, p.tkeys, p.tidx, (uint64_t)(T - 1), p.bad, p.bad + 1);
+        pos, S, nsat, ordered, npairs, lambda_m, scale, p.tkeys, p.tidx, (uint64_t)(T - 1), p.bad, p.bad + 1);
     VISS_LAUNCH_CHECK("unique_insert_kernel");
     unique_compact_kernel<<<(unsigned)((T + COMPACT_SLOTS - 1) / COMPACT_SLOTS), 256, 0, st>>>(
         p.tkeys, p.tidx, T, p.k1, p.i1, (unsigned long long*)p.nsel);
@@ -836,7 +873,7 @@ int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int ordered, doub
   VISS_CUDA(cub::DeviceRadixSort::SortPairs(p.cub, cb, p.k1, p.tkeys, p.i1, p.tidx, n, 0, 63, st));
   if (n > 0) {
     unique_emit_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(p.tidx, p.nsel, pos, S, nsat, ordered,
-                                                                    lambda_m, scale32, u, v, w);
+                                                                    lambda_m, scale, u, v, w);
     VISS_LAUNCH_CHECK("unique_emit_kernel");
   }
   return VISS_OK;
