@@ -79,7 +79,7 @@ static Tuning make_tuning(const viss_tuning* t) {
     r.ctas_per_sm = t->ctas_per_sm > 0 ? t->ctas_per_sm : 0;
     r.vis_split = t->vis_split > 0 ? t->vis_split : 0;
     r.rec_items = t->rec_items > 0 ? t->rec_items : 0;
-    r.tile = t->tile & 3;
+    r.tile = t->tile & 7;
   }
   return r;
 }
@@ -515,7 +515,7 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   rp.K = vis.K; rp.J = sky.J;
   rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
   rp.recon_mask = cfg.recon_mask;
-  rp.small_tile = (tn.tile >> 1) & 1;
+  rp.row_tile = ((tn.tile >> 1) & 1) ? 1 : ((tn.tile >> 2) & 1) ? 2 : 0;
   rp.npb = (int)p.npb;
   rp.nseg = p.nseg;
   rp.nitems = (int)(p.nseg * p.npb);

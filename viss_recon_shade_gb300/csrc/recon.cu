@@ -62,13 +62,14 @@ struct RecSmem {
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
   float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
   int srange[2];
-  int wkeep[REC_THREADS / 32];
+  int wkeep[(REC_THREADS / 32) * ((Q + REC_THREADS - 1) / REC_THREADS)];
   float4 acc[REC_PIX];            // running totals (re, im) and their Kahan compensation per pixel
 };
 
 template <int RM, bool FRAC, bool COMP, int Q>
 __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COMP, Q>& sm, int64_t pb, int64_t kb,
                                            int64_t ke, float2* out, float norm, bool direct) {
+  constexpr int REC_LOAD = (Q + REC_THREADS - 1) / REC_THREADS;  // tile rows per thread in the load
   const int tid = threadIdx.x;
   // a warp owns 32 * REC_TJ consecutive positions: with the spatial order of
   // the geometric passes that is one compact patch of sky
@@ -117,43 +118,55 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     if (RM == RM_GEO) {
       // keep row tid unless its snapshot's all-occluded cone {a, cos ao} holds the whole
       // block: angle(axis, a) + r < ao, i.e. axis.a > cos(ao - r) = cos ao cos r + sin ao sin r
-      bool keep = false;
-      int pk = 0;
-      if (tid < nq) {
-        pk = p.rowsat[tile + tid];
-        const int sn = sat_gm(pk) / p.nsat;
-        const float4 sc = __ldg(p.scones + 2 * (int64_t)sn);
-        keep = true;
-        if (sc.w <= 1.f && bc0.w >= -1.f && sc.w < bc0.w) {  // the cone is wider than the block
-          const float cao = sc.w, sao = sqrtf(fmaxf(0.f, 1.f - cao * cao));
-          const float lim = fmaf(cao, bc0.w, sao * bsin) + 1e-5f;
-          const float d = fmaf(bc0.x, sc.x, fmaf(bc0.y, sc.y, bc0.z * sc.z));
-          keep = !(d > lim);
-        }
-      }
-      static_assert(Q <= REC_THREADS, "at most one row per thread in the geometric tile load");
-      const unsigned bal = __ballot_sync(0xffffffffu, keep);
-      if ((tid & 31) == 0) sm.wkeep[tid >> 5] = __popc(bal);
-      __syncthreads();
-      int off = __popc(bal & ((1u << (tid & 31)) - 1u)), tot = 0;
+      // (REC_LOAD rows per thread, kept rows compacted in order)
+      bool keep[REC_LOAD];
+      int pk[REC_LOAD];
+      unsigned bal[REC_LOAD];
 #pragma unroll
-      for (int w2 = 0; w2 < REC_THREADS / 32; ++w2) {
-        const int c = sm.wkeep[w2];
-        if (w2 < (tid >> 5)) off += c;
-        tot += c;
+      for (int h = 0; h < REC_LOAD; ++h) {
+        const int r = h * REC_THREADS + tid;
+        keep[h] = false;
+        pk[h] = 0;
+        if (r < nq) {
+          pk[h] = p.rowsat[tile + r];
+          const int sn = sat_gm(pk[h]) / p.nsat;
+          const float4 sc = __ldg(p.scones + 2 * (int64_t)sn);
+          keep[h] = true;
+          if (sc.w <= 1.f && bc0.w >= -1.f && sc.w < bc0.w) {  // the cone is wider than the block
+            const float cao = sc.w, sao = sqrtf(fmaxf(0.f, 1.f - cao * cao));
+            const float lim = fmaf(cao, bc0.w, sao * bsin) + 1e-5f;
+            const float d = fmaf(bc0.x, sc.x, fmaf(bc0.y, sc.y, bc0.z * sc.z));
+            keep[h] = !(d > lim);
+          }
+        }
+        bal[h] = __ballot_sync(0xffffffffu, keep[h]);
+        if ((tid & 31) == 0) sm.wkeep[h * (REC_THREADS / 32) + (tid >> 5)] = __popc(bal[h]);
       }
-      if (keep) {
-        const int64_t k = tile + tid;
-        sm.r0[off] = p.rows0[k];
-        sm.r1[off] = p.rows1[k];
-        if (COMP) sm.rf[off] = p.rowsf[k];
-        const int sn = sat_gm(pk) / p.nsat;
-        sm.pk[off] = pk;
-        sm.snap[off] = sn;
-        atomicMin(&sm.srange[0], sn);
-        atomicMax(&sm.srange[1], sn);
+      __syncthreads();
+      int base = 0;
+#pragma unroll
+      for (int h = 0; h < REC_LOAD; ++h) {
+        int off = base + __popc(bal[h] & ((1u << (tid & 31)) - 1u)), tot = 0;
+#pragma unroll
+        for (int w2 = 0; w2 < REC_THREADS / 32; ++w2) {
+          const int c = sm.wkeep[h * (REC_THREADS / 32) + w2];
+          if (w2 < (tid >> 5)) off += c;
+          tot += c;
+        }
+        if (keep[h]) {
+          const int64_t k = tile + h * REC_THREADS + tid;
+          sm.r0[off] = p.rows0[k];
+          sm.r1[off] = p.rows1[k];
+          if (COMP) sm.rf[off] = p.rowsf[k];
+          const int sn = sat_gm(pk[h]) / p.nsat;
+          sm.pk[off] = pk[h];
+          sm.snap[off] = sn;
+          atomicMin(&sm.srange[0], sn);
+          atomicMax(&sm.srange[1], sn);
+        }
+        base += tot;
       }
-      nq = tot;
+      nq = base;
       __syncthreads();
       if (nq == 0) continue;  // the block is hidden from every row of this tile
     }
@@ -338,12 +351,15 @@ static void launch_tile(const ReconParams& p, int ctas_per_sm, cudaStream_t st) 
   recon_fast_kernel<RM, COMP, Q><<<g, REC_THREADS, 0, st>>>(p);
 }
 
-// Row tiles of REC_Q visibilities, or REC_Q / 2 (tuning).
+// Row tiles of REC_Q visibilities, REC_Q / 2 or 2 REC_Q (tuning).
 template <int RM>
 static void launch_rm(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
-  if (p.small_tile) {
+  if (p.row_tile == 1) {
     if (comp) launch_tile<RM, true, REC_Q / 2>(p, ctas_per_sm, st);
     else launch_tile<RM, false, REC_Q / 2>(p, ctas_per_sm, st);
+  } else if (p.row_tile == 2) {
+    if (comp) launch_tile<RM, true, 2 * REC_Q>(p, ctas_per_sm, st);
+    else launch_tile<RM, false, 2 * REC_Q>(p, ctas_per_sm, st);
   } else {
     if (comp) launch_tile<RM, true, REC_Q>(p, ctas_per_sm, st);
     else launch_tile<RM, false, REC_Q>(p, ctas_per_sm, st);
