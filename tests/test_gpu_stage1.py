@@ -110,3 +110,21 @@ def test_unique_uvw_random_positions(V):
     got = V.unique_uvw(pos, 10.0, ordered=True)
     for a, b in zip(got, ref):
         assert np.array_equal(a.cpu().numpy().view(np.int32), b.cpu().numpy().view(np.int32))
+
+
+@pytest.mark.parametrize("nsat,ordered", [(16, True), (32, False), (32, True), (2, True)])
+def test_unique_uvw_other_formation_sizes(V, nsat, ordered):
+    """Other satellite counts (120 and 496 pairs a snapshot, and a single pair):
+    slowly drifting positions, so runs of repeated keys cross chunk boundaries."""
+    rng = np.random.default_rng(nsat)
+    S = 700
+    base = rng.normal(0, 30, (1, nsat, 3))
+    drift = rng.normal(0, 0.02, (1, nsat, 3))
+    pos = (base + drift * np.arange(S)[:, None, None]).astype(np.float32)
+    pos_t = torch.from_numpy(pos).cuda()
+    u, v, w, _, _ = V.baseline_uvw(pos_t, 3.0, ordered=ordered, rounding=True)
+    ref = V.dedup_uvw(*(pair_major(pos_t, x) for x in (u, v, w)))
+    got = V.unique_uvw(pos_t, 3.0, ordered=ordered)
+    assert got[0].numel() == ref[0].numel() > 0
+    for a, b in zip(got, ref):
+        assert np.array_equal(a.cpu().numpy().view(np.int32), b.cpu().numpy().view(np.int32))
