@@ -91,8 +91,11 @@ def max_over_ranks(x: float, ws: int) -> float:
 
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
-    """nvidia-smi clock / throttle-reason sampling during the timed region."""
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi clock / throttle-reason sampling during the timed region (the body of
+    the `with`).  nvidia-smi is started and its first sample awaited before the body
+    runs: its start-up stalls the GPU for a few hundred ms, which must not fall inside a
+    short timed region.  Samples are time-stamped and those around the body kept."""
+    Q = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -100,6 +103,7 @@ class ClockSampler:
         self.gpu = gpu
         self.proc = None
         self.path = None
+        self.t0 = self.t1 = None
 
     def __enter__(self):
         try:
@@ -108,11 +112,19 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
                                          stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            deadline = time.time() + 10.0
+            while time.time() < deadline and self.proc.poll() is None:
+                with open(self.path) as f:
+                    if f.read().count("\n") >= 2:
+                        break
+                time.sleep(0.02)
         except Exception:
             self.proc = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *a):
+        self.t1 = time.time()
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -120,15 +132,25 @@ class ClockSampler:
             except Exception:
                 self.proc.kill()
 
+    def _in_window(self, stamp: str) -> bool:
+        import datetime
+        try:
+            t = datetime.datetime.strptime(stamp.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return True
+        return self.t0 - 0.3 <= t <= self.t1 + 0.3
+
     def summary(self):
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         rows = []
         with open(self.path) as f:
             for r in csv.reader(f):
-                if len(r) >= 9:
+                if len(r) >= 10:
                     rows.append([x.strip() for x in r])
         os.unlink(self.path)
+        window = [r for r in rows if self._in_window(r[0])]
+        rows = [r[1:] for r in (window or rows)]
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -184,7 +206,11 @@ def run_ours(args, ws, rank, local):
         V.vis_dft(cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
         V.recon(cfg, d["u"], d["v"], d["w"], Vout, d["l"], d["m"], d["n"], out=Fout, **geo)
 
+    # warm-up steps run exactly what a timed step runs, the L2 flush included: the first
+    # use of a library kernel on a fresh machine may JIT it (torch's fill kernel for
+    # this GPU, cached afterwards), which must not land in the timed region
     for _ in range(args.warmup):
+        flush.zero_()
         step()
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
@@ -287,6 +313,7 @@ def run_ours(args, ws, rank, local):
     if not args.no_plain:
         pcfg = cfg.with_(precision=V.PREC_PLAIN)
         V.vis_dft(pcfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], out=Vout, **geo)
+        V.recon(pcfg, d["u"], d["v"], d["w"], Vout, d["l"], d["m"], d["n"], out=Fout, **geo)  # warm-up
         torch.cuda.synchronize()
         p0, p1, p2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
         flush.zero_()
@@ -512,6 +539,7 @@ def run_batch(args, ws, rank, local):
     g = b.graph()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     for _ in range(args.warmup):
+        flush.zero_()  # as in a timed step (see run_ours)
         g.replay()
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
