@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
+    ap.add_argument("--no-stage1", action="store_true", help="skip the stage-1 (uvw generation) record")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -351,6 +352,18 @@ def run_ours(args, ws, rank, local):
             "plain": plain, "cpu_baseline": cpu}
     if plain:
         line["speedup_vs_plain"] = round(value / plain["value"], 2)
+    if not args.no_stage1:
+        # stage 1 of the path (positions -> unique uvw) at the reference's own size, for
+        # the record; `--workload stage1` reports it in full
+        del Vout, Fout, flush
+        torch.cuda.empty_cache()
+        K1, n1, ms1, _ = stage1_passes(3, 3)
+        line["stage1"] = {"value": round(K1 / (sum(ms1) * 1e-3) / 1e9, 3), "unit": "G uvw rows/s",
+                          "ms_per_pass": round(sum(ms1), 2), "uvw_rows": K1, "unique_rows": n1,
+                          "stage_ms": {"positions": round(ms1[0], 2), "unique_fused": round(ms1[1], 2)},
+                          "what": "MIncline_generate_uvw_float at its own size (8 satellites, 864,000 samples "
+                                  "an orbit, 140 orbits, 10 MHz): positions + viss_unique_uvw"}
+        torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -630,6 +643,33 @@ def batch_accuracy(d, b, cfg):
 
 
 # ------------------------------------------------------------------ stage 1: orbits -> uvw
+def stage1_passes(steps, warmup):
+    """Timed passes of stage 1 at the reference's MIncline size (positions, then the
+    fused baselines + unique, CUDA events per stage).  Returns (uvw rows, unique rows,
+    mean ms per stage, the last pass's tensors)."""
+    import torch
+    import viss_recon_shade_gb300 as V
+    cfg = V.OrbitConfig()
+    st = torch.cuda.current_stream()
+
+    def step():
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record(st)
+        pos = V.orbit_positions(cfg)
+        ev[1].record(st)
+        uu, vv, ww = V.unique_uvw(pos, 30.0, ordered=True, capacity=1 << 25)
+        ev[2].record(st)
+        torch.cuda.synchronize()
+        K = pos.shape[0] * pos.shape[1] * (pos.shape[1] - 1)
+        return K, uu.numel(), [ev[i].elapsed_time(ev[i + 1]) for i in range(2)], (pos, uu, vv, ww)
+
+    for _ in range(warmup):
+        step()
+    res = [step() for _ in range(steps)]
+    ms = [sum(r[2][i] for r in res) / len(res) for i in range(2)]
+    return res[0][0], res[0][1], ms, res[-1][3]
+
+
 def run_stage1(args, ws, rank, local):
     """--workload stage1: the reference's uvw generation at its own size
     (MIncline_generate_uvw_float.cu: 8 satellites, OrbitRes 864,000, 140 orbits,
@@ -645,28 +685,9 @@ def run_stage1(args, ws, rank, local):
     cfg = V.OrbitConfig()  # the reference's constants
     st = torch.cuda.current_stream()
     lam = 30.0
-
-    def step():
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        ev[0].record(st)
-        pos = V.orbit_positions(cfg)
-        ev[1].record(st)
-        uu, vv, ww = V.unique_uvw(pos, lam, ordered=True, capacity=1 << 25)
-        ev[2].record(st)
-        torch.cuda.synchronize()
-        n = uu.numel()
-        K = pos.shape[0] * pos.shape[1] * (pos.shape[1] - 1)
-        return K, n, [ev[i].elapsed_time(ev[i + 1]) for i in range(2)], (pos, uu, vv, ww)
-
-    for _ in range(args.warmup):
-        step()
-    res = [step() for _ in range(args.steps)]
-    K, n = res[0][0], res[0][1]
-    ms = [sum(r[2][i] for r in res) / len(res) for i in range(2)]
+    K, n, ms, (pos, uu, vv, ww) = stage1_passes(args.steps, args.warmup)
     total = sum(ms)
     # the two-call path once, on the last step's positions, checked against the fused result
-    pos, uu, vv, ww = res[-1][3]
-    del res
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     ev[0].record(st)
     u, v, w, snap, pair = V.baseline_uvw(pos, lam, ordered=True, rounding=True)
