@@ -1,7 +1,6 @@
 """CPU checks of the oracle itself: brute-force numpy on small cases, the
 reference's loop semantics written out literally, and internal identities."""
 import numpy as np
-import pytest
 
 
 def d64(x):

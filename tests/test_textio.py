@@ -4,7 +4,6 @@ to what the reference's `file << value << std::endl` writes
 follows its `while (file >> a >> b ...)` loops."""
 import ctypes as C
 import subprocess
-from pathlib import Path
 
 import numpy as np
 import pytest
