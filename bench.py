@@ -714,8 +714,83 @@ def run_stage1(args, ws, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_textio(args):
+    """--workload textio: the reference-format text files of the 10 MHz headline at its
+    size, through the library's chunk-parallel reader and writer (viss_text_*, all host
+    threads) and the reference's own single-threaded stream loops (restated in the
+    oracle: `uvwFile >> u >> v >> w >> freq`, `file << value << std::endl`).
+    Read: K = 1,835,008 lines `u v w freq` (integer-valued uvw, as the reference's
+    updated_uvw files).  Write: K values one per line (the reference's image-writer
+    format, at K lines for a stable timing).  Files live in /dev/shm when it exists, so
+    the parse and format are timed, not the disk.  No GPU is used."""
+    import ctypes as C
+    import shutil
+    import tempfile
+    import numpy as np
+    from viss_recon_shade_gb300 import _lib as L
+    from oracle import oracle as O
+    K = 1835008
+    rng = np.random.default_rng(0)
+    cols = np.empty((4, K), np.float32)
+    cols[:3] = np.ceil(rng.normal(0, 3000, (3, K)))
+    cols[3] = rng.integers(1, 6, K)
+    img = (rng.standard_normal(K) * 1e3).astype(np.float32)
+    tmp = tempfile.mkdtemp(dir="/dev/shm" if os.path.isdir("/dev/shm") else None)
+    try:
+        fin, fo1, fo2 = (os.path.join(tmp, n).encode() for n in ("uvw.txt", "F_ours.txt", "F_ref.txt"))
+        L.check(L.lib.viss_text_write_floats(fin, 4, cols.ctypes.data_as(C.c_void_p), K, K), "write input")
+        in_bytes = os.path.getsize(fin)
+        out = np.empty((4, K), np.float32)
+        nrows, hv = C.c_int64(0), C.c_int64(0)
+
+        def ours_read():
+            L.check(L.lib.viss_text_read_floats(fin, 0, 4, out.ctypes.data_as(C.c_void_p), K, C.byref(nrows),
+                                                C.byref(hv)), "viss_text_read_floats")
+
+        def ours_write():
+            L.check(L.lib.viss_text_write_floats(fo1, 1, img.ctypes.data_as(C.c_void_p), K, K),
+                    "viss_text_write_floats")
+
+        def timed(fn, reps):
+            fn()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            return (time.perf_counter() - t0) / reps
+
+        t_read = timed(ours_read, args.steps)
+        t_write = timed(ours_write, args.steps)
+        ref_cols, nref = O.text_read_stream(fin.decode(), 4, K)
+        same_read = nref == K and np.array_equal(ref_cols, out) and np.array_equal(out, cols)
+        t_rread = timed(lambda: O.text_read_stream(fin.decode(), 4, K), 1)
+        t_rwrite = timed(lambda: O.text_write_stream(fo2.decode(), img), 1)
+        with open(fo1, "rb") as a, open(fo2, "rb") as b:
+            same_write = a.read() == b.read()
+        out_bytes = os.path.getsize(fo1)
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    mb = 1e6
+    line = {"metric": "reference-format text I/O (parse + format), MB/s of file text", "value":
+            round((in_bytes + out_bytes) / (t_read + t_write) / mb, 1), "unit": "MB/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": 1, "ms_per_step": round((t_read + t_write) * 1e3, 2),
+            "higher_is_better": True, "scaling": "none", "vs_baseline": None, "dtype": "text", "data": "synthetic",
+            "config": {"workload": "textio", "read_lines": K, "read_bytes": in_bytes, "write_lines": K,
+                       "write_bytes": out_bytes, "threads": os.cpu_count(), "tmpfs": tmp.startswith("/dev/shm")},
+            "read": {"ms": round(t_read * 1e3, 2), "MB_per_s": round(in_bytes / t_read / mb, 1),
+                     "reference_ms": round(t_rread * 1e3, 2), "identical_values": bool(same_read)},
+            "write": {"ms": round(t_write * 1e3, 2), "MB_per_s": round(out_bytes / t_write / mb, 1),
+                      "reference_ms": round(t_rwrite * 1e3, 2), "identical_bytes": bool(same_write)},
+            "cpu_baseline": {"value": round((in_bytes + out_bytes) / (t_rread + t_rwrite) / mb, 1), "unit": "MB/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "the same files through the reference's stream loops (oracle)"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
+    if args.workload == "textio":
+        run_textio(args)
+        return
     ws, rank, local = dist_setup()
     from viss_recon_shade_gb300.synth import BATCH_WORKLOADS
     if args.impl == "reference":

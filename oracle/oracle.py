@@ -71,6 +71,8 @@ def lib():
         _lib.oracle_uvw.restype = C.c_int64
         _lib.oracle_uvw_f64.restype = C.c_int64
         _lib.oracle_dedup_uvw.restype = C.c_int64
+        _lib.oracle_text_read_stream.restype = C.c_int64
+        _lib.oracle_text_write_stream.restype = C.c_int64
         _lib.oracle_shade_windows.restype = C.c_double
         _lib.oracle_max_threads.restype = C.c_int
     return _lib
@@ -253,3 +255,16 @@ def nxq(NX, J):
 
 def max_threads() -> int:
     return int(lib().oracle_max_threads())
+
+
+def text_read_stream(path, ncols, cap):
+    """The reference's single-threaded `ifstream >>` reading loop; columns [ncols, rows]."""
+    out = np.zeros((ncols, cap), np.float32)
+    n = lib().oracle_text_read_stream(str(path).encode(), C.c_int(ncols), _p(out), C.c_int64(cap))
+    return out[:, :min(n, cap)], n
+
+
+def text_write_stream(path, values):
+    """The reference's `file << value << std::endl` writing loop."""
+    values = np.ascontiguousarray(values, dtype=np.float32)
+    return lib().oracle_text_write_stream(str(path).encode(), _p(values), C.c_int64(values.size))

@@ -33,6 +33,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
 #include <tuple>
 #include <vector>
 #include <omp.h>
@@ -708,3 +709,33 @@ ORACLE_API void oracle_nxq(const float* NX, int64_t X, int64_t J, int32_t* count
 }
 
 ORACLE_API int oracle_max_threads(void) { return omp_get_max_threads(); }
+
+// ===========================================================================
+// The reference's text I/O, restated as the CPU baseline of the text I/O path:
+// one thread, formatted stream extraction of `ncols` floats per line until it
+// fails (vissGen10M_shade.cu:354-365, `uvwFile >> u >> v >> w >> freq`), and one
+// `file << value << std::endl` per value (:573-578).  Column c of row r lives at
+// cols[c * cap + r].  Returns the rows read / written, -1 if the file does not open.
+// ===========================================================================
+ORACLE_API int64_t oracle_text_read_stream(const char* path, int ncols, float* cols, int64_t cap) {
+  std::ifstream f(path);
+  if (!f.is_open() || ncols < 1 || ncols > 8) return -1;
+  float x[8];
+  int64_t r = 0;
+  for (;;) {
+    int c = 0;
+    while (c < ncols && (f >> x[c])) ++c;
+    if (c < ncols) break;
+    if (r < cap)
+      for (int k = 0; k < ncols; ++k) cols[k * cap + r] = x[k];
+    ++r;
+  }
+  return r;
+}
+
+ORACLE_API int64_t oracle_text_write_stream(const char* path, const float* values, int64_t n) {
+  std::ofstream f(path);
+  if (!f.is_open()) return -1;
+  for (int64_t i = 0; i < n; ++i) f << values[i] << std::endl;
+  return n;
+}
