@@ -678,7 +678,9 @@ def run_stage1(args, ws, rank, local):
     two-call path (viss_baseline_uvw + viss_dedup_uvw, 2.26e9 rows written and
     read back; the pair-major transpose between them untimed) is timed once
     afterwards, checked against the fused result and reported beside it.
-    Reported: uvw rows per second, inputs generated on the device."""
+    Reported: uvw rows per second, inputs generated on the device.  The shade windows
+    of the unique rows (the pipeline's next stage) are timed and reported beside it."""
+    import numpy as np
     import torch
     import viss_recon_shade_gb300 as V
     cfg = V.OrbitConfig()  # the reference's constants
@@ -701,6 +703,27 @@ def run_stage1(args, ws, rank, local):
     two = [ev[i].elapsed_time(ev[i + 1]) for i in range(2)]
     del u, v, w, u2, v2, w2
     torch.cuda.empty_cache()
+    # stage 2 of the reference's pipeline on this output: the shade windows of every
+    # unique uvw at the 10 MHz grid (shade10M: RES 20940), and the oracle's FP32
+    # restatement of the reference's kernels on one host thread on a 1M-row sample
+    RES = 20940
+    V.shade_windows(uu, vv, ww, RES)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(3):
+        shade, mean_r = V.shade_windows(uu, vv, ww, RES)
+    e1.record(st)
+    torch.cuda.synchronize()
+    shade_ms = e0.elapsed_time(e1) / 3
+    from oracle import oracle as O
+    ns = min(n, 1 << 20)
+    hu, hv, hw = (x[:ns].cpu().numpy() for x in (uu, vv, ww))
+    t0 = time.perf_counter()
+    ref, _ = O.shade_windows(hu, hv, hw, RES, mean_r=mean_r, mode=1)
+    cpu_s = time.perf_counter() - t0
+    diff = np.abs(shade[:ns].cpu().numpy().astype(np.int64) - ref)
+    off_by = int((np.minimum(diff, RES - diff) > 0).sum())
     line = {"metric": "uvw rows/s, orbit positions + baseline uvw + sort/unique, 1 GB300",
             "value": round(K / (total * 1e-3) / 1e9, 3), "unit": "G uvw rows/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total, 2), "higher_is_better": True, "scaling": "weak",
@@ -709,7 +732,12 @@ def run_stage1(args, ws, rank, local):
                        "orbit_counts": cfg.orbit_counts, "snapshots": cfg.snapshots, "uvw_rows": K,
                        "unique_rows": n, "freq_hz": 1e7},
             "stage_ms": {"positions": round(ms[0], 2), "unique_fused": round(ms[1], 2)},
-            "two_call_ms": {"baselines": round(two[0], 2), "dedup": round(two[1], 2), "identical": same}}
+            "two_call_ms": {"baselines": round(two[0], 2), "dedup": round(two[1], 2), "identical": same},
+            "shade_windows": {"rows": n, "res": RES, "ms": round(shade_ms, 3),
+                              "G_rows_per_s": round(n / (shade_ms * 1e-3) / 1e9, 2),
+                              "cpu_baseline": {"value": round(ns / cpu_s / 1e9, 4), "unit": "G rows/s", "cores": 1,
+                                               "kind": "port", "sample": f"{ns} rows, FP32 restatement (oracle)"},
+                              "window_ends_differing_from_oracle": off_by}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
