@@ -128,3 +128,35 @@ def test_unique_uvw_other_formation_sizes(V, nsat, ordered):
     assert got[0].numel() == ref[0].numel() > 0
     for a, b in zip(got, ref):
         assert np.array_equal(a.cpu().numpy().view(np.int32), b.cpu().numpy().view(np.int32))
+
+
+def test_unique_uvw_count_only_and_short_capacity(V):
+    """Through the C ABI: capacity 0 only counts; a nonzero capacity below the count
+    returns VISS_ERR_RANGE with the count set; the exact capacity then succeeds."""
+    import ctypes as C
+    from viss_recon_shade_gb300 import _lib as L
+    pos = V.orbit_positions(V.OrbitConfig(orbit_res=3600, orbit_counts=2)).contiguous()
+    S, nsat = pos.shape[0], pos.shape[1]
+    nb = L.lib.viss_unique_uvw_workspace(S, nsat, 1)
+    ws = torch.empty(nb, dtype=torch.uint8, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    cnt = C.c_int64(-1)
+    rc = L.lib.viss_unique_uvw(C.c_void_p(pos.data_ptr()), S, nsat, 1, 30.0, None, None, None, 0, C.byref(cnt),
+                               C.c_void_p(ws.data_ptr()), nb, st)
+    assert rc == L.VISS_OK and cnt.value > 1
+    n = cnt.value
+    u, v, w = (torch.empty(n, dtype=torch.float32, device="cuda") for _ in range(3))
+    ptrs = [C.c_void_p(x.data_ptr()) for x in (u, v, w)]
+    rc = L.lib.viss_unique_uvw(C.c_void_p(pos.data_ptr()), S, nsat, 1, 30.0, *ptrs, n - 1, C.byref(cnt),
+                               C.c_void_p(ws.data_ptr()), nb, st)
+    assert rc == L.VISS_ERR_RANGE and cnt.value == n
+    rc = L.lib.viss_unique_uvw(C.c_void_p(pos.data_ptr()), S, nsat, 1, 30.0, *ptrs, n, C.byref(cnt),
+                               C.c_void_p(ws.data_ptr()), nb, st)
+    assert rc == L.VISS_OK and cnt.value == n
+    ref = V.unique_uvw(pos, 30.0, ordered=True)
+    for a, b in zip((u, v, w), ref):
+        assert torch.equal(a.view(torch.int32), b.view(torch.int32))
+    # a workspace one byte short is refused
+    rc = L.lib.viss_unique_uvw(C.c_void_p(pos.data_ptr()), S, nsat, 1, 30.0, *ptrs, n, C.byref(cnt),
+                               C.c_void_p(ws.data_ptr()), nb - 1, st)
+    assert rc == L.VISS_ERR_WORKSPACE
