@@ -214,3 +214,30 @@ def test_vissGen1M_fine_map(oracle, tmp_path):
     Ffine = Fo.real[NX.astype(np.int64) - 1]  # expanded to the fine grid
     assert F.shape == (res * res,)
     assert np.abs(F - Ffine).max() / np.abs(Ffine).max() < 2e-5
+
+
+def test_vissGen1M_shade_accurate_dropin(oracle, tmp_path):
+    """vissGen1M_shade_accurate: the 1M fine-map flow with the fine brightness truncated
+    to int (vissGen1M_shade_accurate.cu:115), written expanded as
+    F_recon_1M_accu/Ex{p}frequency1M.txt (:571-585)."""
+    res, K = 64, 1024
+    fd = tmp_path / "frequency_1M"
+    l, m, n, FF, NX, J = make_map_sky_dir(fd, res, seed=13)
+    u, v, w, raw = synth_uvw_shade(K, res, seed=14)
+    np.savetxt(fd / "uvw1frequency1M.txt", np.stack([u, v, w], -1), fmt="%g")
+    np.savetxt(fd / "shadeM1frequency1M.txt", raw, fmt="%d")
+    run([BIN / "vissGen1M_shade_accurate", "--res", res], tmp_path)
+    F = read_col(tmp_path / "F_recon_1M_accu" / "Ex1frequency1M.txt")
+    cl, nq = oracle.nxq(NX, J)
+    M = oracle.normalise_shade(raw)
+    V = oracle.vis_dft_nxq(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0, trunc=True), u, v, w, l, m, n,
+                           FF, nq.astype(np.float32), cl, shade=M)
+    Fo = oracle.recon(oracle.make_cfg(res=res, recon_ref_mask=True, norm=1.0 / K), u, v, w, None,
+                      V.astype(np.complex64), l, m, n, shade=M)
+    Ffine = Fo.real[NX.astype(np.int64) - 1]
+    assert F.shape == (res * res,)
+    assert np.abs(F - Ffine).max() / np.abs(Ffine).max() < 2e-5
+    # the truncation matters on this sky: the untruncated brightness gives another image
+    V2 = oracle.vis_dft_nxq(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0), u, v, w, l, m, n, FF,
+                            nq.astype(np.float32), cl, shade=M)
+    assert np.abs(V2 - V).max() > 1e-3 * np.abs(V).max()

@@ -5,6 +5,9 @@
 //
 //   vissGen10M_shade   vissGen10M_shade.cu:178-611 (+ _optim1/_optim2 file names)
 //   vissGen1M_shade    vissGen1M_shade_optim1.cu:265-726 (uvwMap130 weights, NX expansion)
+//   vissGen1M_shade_accurate  vissGen1M_shade_accurate.cu:95-620 (int-truncated
+//                      brightness, F_recon_1M_accu/Ex{p}frequency1M.txt; the reference
+//                      file itself does not compile: `totalnode` is undeclared at :300)
 //   shade1M/10M/30M    shade1M.cu:130-280, shade10M.cu, shade30M.cu
 //   MIncline_generate_uvw_float   MIncline_generate_uvw_float.cu:184-484
 //
@@ -217,7 +220,8 @@ int vissgen(const Args& a, bool tenM) {
       CHECKC(cudaDeviceSynchronize());
     }
   }
-  const std::string outdir = tenM ? root + "/F_recon_10M/" : root + "/F_recon_1M/";
+  const bool accurate = variant == "accurate";
+  const std::string outdir = tenM ? root + "/F_recon_10M/" : root + (accurate ? "/F_recon_1M_accu/" : "/F_recon_1M/");
   mkdir_p(outdir);
   for (int p = start_period; p < days; ++p) {
     const double t0 = now();
@@ -267,7 +271,8 @@ int vissgen(const Args& a, bool tenM) {
       return 1;
     }
     const double t1 = now();
-    const int var = variant == "plain" ? VISS_VARIANT_PLAIN : VISS_VARIANT_OPTIM;
+    // plain and accurate truncate the fine brightness to int (vissGen1M_shade_accurate.cu:115)
+    const int var = variant == "plain" || accurate ? VISS_VARIANT_PLAIN : VISS_VARIANT_OPTIM;
     if (identity || tenM) {
       CHECKV(viss_visscal((int)K, (int)J, RES, dFF.p, dV.p, du.p, dv.p, dw.p, dl_.p, dm_.p, dn_.p, dM1.p, dM2.p,
                           dM3.p, dM4.p, identity ? nullptr : dNXqf.p, identity ? nullptr : dcl.p, d, d, d, var, mask,
@@ -311,8 +316,10 @@ int vissgen(const Args& a, bool tenM) {
       for (int64_t j = 0; j < J; ++j) re[j] = F[2 * j];
       CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), J, J));
     } else {
-      // expanded to the fine grid: F[NX[c]-1] (vissGen1M_shade_optim1.cu:680-684)
-      out = outdir + "F" + std::to_string(p + 1) + "_" + variant + ".txt";
+      // expanded to the fine grid: F[NX[c]-1] (vissGen1M_shade_optim1.cu:680-684,
+      // vissGen1M_shade_accurate.cu:571-585 as Ex{p}frequency1M.txt)
+      out = accurate ? outdir + "Ex" + std::to_string(p + 1) + dur + ".txt"
+                     : outdir + "F" + std::to_string(p + 1) + "_" + variant + ".txt";
       std::vector<float> re(X);
       for (int64_t c = 0; c < X; ++c) re[c] = F[2 * ((int64_t)NX[c] - 1)];
       CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
@@ -448,13 +455,14 @@ int main(int argc, char** argv) {
   if (prog.rfind("vissGen1M", 0) == 0) {
     Args b = a;
     if (prog.find("optim2") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "optim2";
+    if (prog.find("accurate") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "accurate";
     return vissgen(b, false);
   }
   if (prog == "shade1M" || prog == "shade10M" || prog == "shade30M") return shade(a, prog);
   if (prog.rfind("MIncline", 0) == 0) return mincline(a);
   std::fprintf(stderr,
                "usage: viss_dropin {vissGen10M_shade|vissGen10M_shade_optim1|vissGen10M_shade_optim2|"
-               "vissGen1M_shade_optim1|vissGen1M_shade_optim2|shade1M|shade10M|shade30M|"
+               "vissGen1M_shade_optim1|vissGen1M_shade_optim2|vissGen1M_shade_accurate|shade1M|shade10M|shade30M|"
                "MIncline_generate_uvw_float} [--root DIR] [--flag value ...]\n");
   return 2;
 }
