@@ -190,6 +190,16 @@ VISS_API size_t viss_nxq_workspace(int64_t X, int64_t J);
 VISS_API int viss_nxq(const float* NX, int64_t X, int64_t J, int32_t* countLoc, int32_t* NXq, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* viss_vis_dft with a REF mask whose window tests win_index[j] (J int32, may be negative
+ * or beyond the grid) for pixel j instead of j itself.  vissGen1M_shade_appro.cu:113-118
+ * tests NX[j] - 1, the fine-array entry read at the coarse index; its write of 240 into
+ * the shared brightness array is a race between threads and is not reproduced: the
+ * occluded value replaces the brightness for that (visibility, pixel) term only. */
+VISS_API size_t viss_vis_dft_windowed_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J);
+VISS_API int viss_vis_dft_windowed(const viss_dft_cfg* cfg, const viss_sky* sky, const int32_t* win_index,
+                                   const viss_vis_set* vis, float* V, void* workspace, size_t workspace_bytes,
+                                   void* stream);
+
 /* Input problems a pass records instead of reading out of bounds (a pass never
  * synchronises to look): after the pass has completed, reads the flag word at
  * the start of its workspace (synchronises `stream`).  Bits: 1 = |uvw| >= 2^30,

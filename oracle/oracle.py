@@ -64,7 +64,7 @@ def lib():
     if _lib is None:
         build()
         _lib = C.CDLL(str(LIB))
-        for name in ("oracle_vis_dft", "oracle_vis_dft_nxq", "oracle_recon", "oracle_vis_plain_f32",
+        for name in ("oracle_vis_dft", "oracle_vis_dft_windex", "oracle_vis_dft_nxq", "oracle_recon", "oracle_vis_plain_f32",
                      "oracle_recon_plain_f32", "oracle_geo_mask", "oracle_orbit_positions",
                      "oracle_orbit_positions_f64"):
             getattr(_lib, name).restype = C.c_int
@@ -115,6 +115,17 @@ def vis_dft(cfg: DftCfg, u, v, w, l, m, n, bright, shade=None, geo=None, nthread
     lib().oracle_vis_dft(C.byref(cfg), _p(u), _p(v), _p(w), C.c_int64(K), _p(shade),
                          C.byref(geo) if geo is not None else None, _p(l), _p(m), _p(n), _p(bright),
                          C.c_int64(J), _p(out), C.c_int(nthreads))
+    return out[:, 0] + 1j * out[:, 1]
+
+
+def vis_dft_windex(cfg: DftCfg, u, v, w, l, m, n, bright, shade, widx, nthreads=0):
+    """vis_dft with the REF window tested on widx[j] instead of j; complex128[K]."""
+    u, v, w, l, m, n, bright = map(_f32, (u, v, w, l, m, n, bright))
+    shade, widx = _i32(shade), _i32(widx)
+    K, J = u.size, l.size
+    out = np.zeros((K, 2), np.float64)
+    lib().oracle_vis_dft_windex(C.byref(cfg), _p(u), _p(v), _p(w), C.c_int64(K), _p(shade), _p(widx), _p(l), _p(m),
+                                _p(n), _p(bright), C.c_int64(J), _p(out), C.c_int(nthreads))
     return out[:, 0] + 1j * out[:, 1]
 
 

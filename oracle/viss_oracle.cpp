@@ -157,13 +157,15 @@ typedef struct oracle_geo {
 
 namespace {
 
+// widx: the fine index the REF window tests for pixel j (NULL: j itself)
 inline bool term_masked(const oracle_dft_cfg* cfg, const int32_t* shade, const oracle_geo* geo,
-                        const float* l, const float* m, const float* n, int64_t k, int64_t j) {
+                        const float* l, const float* m, const float* n, int64_t k, int64_t j,
+                        const int32_t* widx = nullptr) {
   switch (cfg->mask_mode) {
     case MASK_REF_QUIRK:
     case MASK_REF_INTENDED: {
       const int32_t* M = shade + 4 * k;
-      return ref_window_hit_fast(j, cfg->res, M[0], M[1], M[2], M[3], cfg->mask_mode);
+      return ref_window_hit(widx ? (int64_t)widx[j] : j, cfg->res, M[0], M[1], M[2], M[3], cfg->mask_mode);
     }
     case MASK_GEOMETRIC: {
       const int32_t s = geo->snap[k];
@@ -203,6 +205,37 @@ ORACLE_API int oracle_vis_dft(const oracle_dft_cfg* cfg, const float* u, const f
       double c = bright[j];
       if (cfg->trunc_brightness) c = (double)(int)bright[j];
       if (cfg->mask_mode != MASK_NONE && term_masked(cfg, shade, geo, l, m, n, k, j))
+        c = cfg->occluded_value;
+      if (c == 0.0) continue;
+      const double t = s * (uk * (double)l[j] + vk * (double)m[j] + wk * ((double)n[j] + noff));
+      const double x = 2.0 * kPi * frac_turns(t);
+      re += c * std::cos(x);
+      im -= c * std::sin(x);
+    }
+    V[2 * k] = re;
+    V[2 * k + 1] = im;
+  }
+  return 0;
+}
+
+// The same with the REF window tested on widx[j] instead of the pixel index j: the
+// appro program's visscal (vissGen1M_shade_appro.cu:113-118) tests NX[j] - 1, the
+// fine-array entry at the coarse index, against the window of row k (its write of
+// 240 into the shared brightness is a race and is not followed: the occluded
+// value replaces C_j for that term only).
+ORACLE_API int oracle_vis_dft_windex(const oracle_dft_cfg* cfg, const float* u, const float* v, const float* w,
+                                     int64_t K, const int32_t* shade, const int32_t* widx, const float* l,
+                                     const float* m, const float* n, const float* bright, int64_t J, double* V,
+                                     int nthreads) {
+  const double s = cfg->phase_scale, noff = cfg->n_offset;
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+  for (int64_t k = 0; k < K; ++k) {
+    const double uk = u[k], vk = v[k], wk = w[k];
+    double re = 0.0, im = 0.0;
+    for (int64_t j = 0; j < J; ++j) {
+      double c = bright[j];
+      if (cfg->trunc_brightness) c = (double)(int)bright[j];
+      if (cfg->mask_mode != MASK_NONE && term_masked(cfg, shade, nullptr, l, m, n, k, j, widx))
         c = cfg->occluded_value;
       if (c == 0.0) continue;
       const double t = s * (uk * (double)l[j] + vk * (double)m[j] + wk * ((double)n[j] + noff));

@@ -313,3 +313,43 @@ def test_linearity_and_adjoint_large(V):
     # scale of the identity: |<Ax, y>| <= ||Ax|| ||y|| (the sum itself cancels heavily)
     scale = A1.abs().double().norm().item() * y.abs().double().norm().item()
     assert abs(lhs - rhs) / scale < 1e-5
+
+
+@pytest.mark.parametrize("mode", ["quirk", "intended"])
+@pytest.mark.parametrize("prec", ["fast", "plain"])
+def test_vis_windowed_index(V, oracle, mode, prec):
+    """viss_vis_dft_windowed: the REF window tests win_index[j] (a shuffled grid index,
+    some negative or past the grid) instead of j; exact counts with zero phase and the
+    FP64 oracle otherwise.  An identity index reproduces viss_vis_dft."""
+    K, J, res = 2048, 3000, 300
+    rng = np.random.default_rng(21)
+    widx = rng.permutation(J).astype(np.int32)
+    widx[::37] = -1 - rng.integers(0, 5, widx[::37].size)
+    widx[5::41] = J + rng.integers(0, 900, widx[5::41].size)
+    l, m, n, b = sky(J)
+    shade = shade_windows_synth(K, res, seed=10)
+    mm = V.MASK_REF_QUIRK if mode == "quirk" else V.MASK_REF_INTENDED
+    p = V.PREC_FAST if prec == "fast" else V.PREC_PLAIN
+    # zero phase, brightness 0, occluded 1: V_k counts the pixels whose index the window holds
+    z = np.zeros(K, np.float32)
+    cfg0 = V.DftConfig(mask=mm, precision=p, res=res, occluded_value=1.0)
+    Vc = V.vis_dft_windowed(cfg0, cu(z), cu(z), cu(z), *map(cu, (l, m, n)), cu(np.zeros(J, np.float32)), cu(widx),
+                            cu(shade)).cpu().numpy()
+    ks = range(0, K, 61)
+    counts = np.array([sum(oracle_hit(int(widx[j]), res, *shade[k], mm) for j in range(J)) for k in ks])
+    assert np.array_equal(np.round(Vc.real[::61]).astype(np.int64), counts)
+    assert counts.max() > 0
+    # brightness and phase against FP64
+    u, v, w = uvw_int(K, 800.0)
+    cfg = V.DftConfig(mask=mm, precision=p, res=res, occluded_value=240.0)
+    Vg = V.vis_dft_windowed(cfg, *map(cu, (u, v, w, l, m, n, b)), cu(widx), cu(shade)).cpu().numpy()
+    Vo = oracle.vis_dft_windex(oracle.make_cfg(mask_mode=mm, res=res, occluded_value=240.0), u, v, w, l, m, n, b,
+                               shade, widx)
+    rms, mx = errs(Vg, Vo)
+    tol = (TOL_RMS, TOL_MAX) if prec == "fast" else (5e-4, 5e-3)
+    assert rms <= tol[0] and mx <= tol[1], (mode, prec, rms, mx)
+    # identity index: the ordinary pass
+    Vi = V.vis_dft_windowed(cfg, *map(cu, (u, v, w, l, m, n, b)), cu(np.arange(J, dtype=np.int32)),
+                            cu(shade)).cpu().numpy()
+    Vn = V.vis_dft(cfg, *map(cu, (u, v, w, l, m, n, b)), shade=cu(shade)).cpu().numpy()
+    assert np.abs(Vi - Vn).max() <= 1e-6 * np.abs(Vn).max()

@@ -241,3 +241,40 @@ def test_vissGen1M_shade_accurate_dropin(oracle, tmp_path):
     V2 = oracle.vis_dft_nxq(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0), u, v, w, l, m, n, FF,
                             nq.astype(np.float32), cl, shade=M)
     assert np.abs(V2 - V).max() > 1e-3 * np.abs(V).max()
+
+
+def test_vissGen1M_shade_appro_dropin(oracle, tmp_path):
+    """vissGen1M_shade_appro: coarse brightness C_j = mean of FF over NX == j + 1
+    (computeC), the window tested on NX[j] - 1 (the fine-array entry at the coarse
+    index, vissGen1M_shade_appro.cu:113-118; the 240 replaces C_j for that term only,
+    the reference's shared write being a race), d = (float)2 RES / (RES - 1), no recon
+    mask, F / K expanded as F_recon_1M_appro/Ex{p}frequency1M.txt."""
+    res, K = 64, 1024
+    fd = tmp_path / "frequency_1M"
+    l, m, n, FF, NX, J = make_map_sky_dir(fd, res, seed=15)
+    u, v, w, raw = synth_uvw_shade(K, res, seed=16)
+    np.savetxt(fd / "uvw1frequency1M.txt", np.stack([u, v, w], -1), fmt="%g")
+    np.savetxt(fd / "shadeM1frequency1M.txt", raw, fmt="%d")
+    run([BIN / "vissGen1M_shade_appro", "--res", res], tmp_path)
+    F = read_col(tmp_path / "F_recon_1M_appro" / "Ex1frequency1M.txt")
+    csum = np.zeros(J, np.float32)
+    cnt = np.zeros(J, np.int64)
+    for i in range(NX.size):  # float sums in fine-index order, as computeC
+        q = int(NX[i]) - 1
+        csum[q] = np.float32(csum[q] + FF[i])
+        cnt[q] += 1
+    C = np.where(cnt > 0, csum / np.maximum(cnt, 1).astype(np.float32), 0).astype(np.float32)
+    widx = (NX[:J].astype(np.int64) - 1).astype(np.int32)
+    d = float(np.float32(2 * res) / np.float32(res - 1))
+    M = oracle.normalise_shade(raw)
+    Vo = oracle.vis_dft_windex(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0, phase_scale=1.0 / d,
+                                               n_offset=0.0), u, v, w, l, m, n, C, M, widx)
+    Fo = oracle.recon(oracle.make_cfg(phase_scale=1.0 / d, n_offset=0.0, norm=1.0 / K), u, v, w, None,
+                      Vo.astype(np.complex64), l, m, n)
+    Ffine = Fo.real[NX.astype(np.int64) - 1]
+    assert F.shape == (res * res,)
+    assert np.abs(F - Ffine).max() / np.abs(Ffine).max() < 2e-5
+    # the window on NX[j] - 1 is not the window on j: the masks differ on this sky
+    Vj = oracle.vis_dft_windex(oracle.make_cfg(mask_mode=1, res=res, occluded_value=240.0, phase_scale=1.0 / d,
+                                               n_offset=0.0), u, v, w, l, m, n, C, M, np.arange(J, dtype=np.int32))
+    assert np.abs(Vj - Vo).max() > 1e-3 * np.abs(Vo).max()

@@ -102,6 +102,8 @@ _SIGS = {
                                    C.POINTER(Geometry), _P, _P, C.c_size_t, _P]),
     "viss_workspace_flags": (C.c_int, [_P, C.POINTER(C.c_int32), _P]),
     "viss_workspace_limb_count": (C.c_int, [_P, C.POINTER(C.c_int64), _P]),
+    "viss_vis_dft_windowed_workspace": (C.c_size_t, [_P, C.c_int64, C.c_int64]),
+    "viss_vis_dft_windowed": (C.c_int, [_P, _P, _P, _P, _P, _P, C.c_size_t, _P]),
     "viss_nxq_workspace": (C.c_size_t, [C.c_int64, C.c_int64]),
     "viss_nxq": (C.c_int, [_P, C.c_int64, C.c_int64, _P, _P, _P, C.c_size_t, _P]),
     "viss_visscal": (C.c_int, [C.c_int, C.c_int, C.c_int, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P,

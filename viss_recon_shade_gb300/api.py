@@ -126,6 +126,28 @@ def vis_dft(cfg: DftConfig, u, v, w, l, m, n, bright, shade=None, snap=None, pai
     return out
 
 
+def vis_dft_windowed(cfg: DftConfig, u, v, w, l, m, n, bright, win_index, shade,
+                     out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """vis_dft with a REF mask whose window tests win_index[j] for pixel j (the appro
+    program's NX[j] - 1); returns complex64 V[K]."""
+    K, J = u.numel(), l.numel()
+    u, v, w = (_dev(x, torch.float32, nm, K) for x, nm in ((u, "u"), (v, "v"), (w, "w")))
+    l, m, n, bright = (_dev(x, torch.float32, nm, J) for x, nm in ((l, "l"), (m, "m"), (n, "n"), (bright, "bright")))
+    win_index = _dev(win_index, torch.int32, "win_index", J)
+    shade = _dev(shade, torch.int32, "shade", K, 4)
+    if out is None:
+        out = torch.empty(K, dtype=torch.complex64, device=u.device)
+    c = cfg.c(K)
+    ws_bytes = L.lib.viss_vis_dft_windowed_workspace(C.byref(c), K, J)
+    ws = _workspace(ws_bytes, u.device)
+    sky = L.Sky(l.data_ptr(), m.data_ptr(), n.data_ptr(), bright.data_ptr(), J)
+    vs = L.VisSet(u.data_ptr(), v.data_ptr(), w.data_ptr(), None, _ptr(shade), None, None, K)
+    L.check(L.lib.viss_vis_dft_windowed(C.byref(c), C.byref(sky), _ptr(win_index), C.byref(vs),
+                                        C.c_void_p(out.data_ptr()), _ptr(ws), ws_bytes, _stream()),
+            "viss_vis_dft_windowed")
+    return out
+
+
 def recon(cfg: DftConfig, u, v, w, V, l, m, n, wgt=None, shade=None, snap=None, pair=None, sat_pos=None,
           out: Optional[torch.Tensor] = None) -> torch.Tensor:
     """Direct-DFT reconstruction; returns complex64 F[J] (replaces imagerecon)."""

@@ -87,7 +87,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
 
 # Drop-in programs with the reference's names (one binary, dispatched on argv[0]).
 TOOL_NAMES = ["vissGen10M_shade", "vissGen10M_shade_optim1", "vissGen10M_shade_optim2", "vissGen1M_shade_optim1",
-              "vissGen1M_shade_optim2", "vissGen1M_shade_accurate", "shade1M", "shade10M", "shade30M",
+              "vissGen1M_shade_optim2", "vissGen1M_shade_accurate", "vissGen1M_shade_appro", "shade1M", "shade10M", "shade30M",
               "MIncline_generate_uvw_float"]
 
 

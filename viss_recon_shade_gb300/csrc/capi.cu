@@ -96,6 +96,8 @@ struct VisPlan {
   int64_t K = 0, J = 0, Jpad = 0, Kpad = 0, nrb = 0, jchunk = 0, nsd = 0, X = 0;
   int nsplit = 1;
   bool geo = false, ref = false, comp = false, plain = false, map = false;
+  bool windexed = false;  // REF windows test a per-pixel index (viss_vis_dft_windowed)
+  int2* rrng = nullptr;
   float* mbase = nullptr;
   int4* mbox = nullptr;
   int2 *mmem = nullptr, *mtile = nullptr;
@@ -136,14 +138,16 @@ struct VisPlan {
         mscratch_bytes = fine_map_scratch(J);
         mscratch = c.take<char>(mscratch_bytes);
       }
+      if (windexed && ref) rrng = c.take<int2>(Jpad / VIS_P);
     }
     bytes = c.size();
   }
 };
 
 static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64_t J, const viss_geometry* geo,
-                     const Tuning& tn, const viss_fine_map* map = nullptr) {
+                     const Tuning& tn, const viss_fine_map* map = nullptr, bool windexed = false) {
   p.K = bt.ch.row_off[bt.ch.nch]; p.J = J;
+  p.windexed = windexed;
   p.map = map != nullptr;
   p.X = map ? map->X : 0;
   p.plain = cfg.precision == VISS_PREC_PLAIN;
@@ -347,9 +351,10 @@ static viss_vis_set channel_rows(const viss_vis_set& vis, int64_t r0, int64_t r1
 
 int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[3], const viss_sky& sky,
                  const viss_vis_set& vis, const Batch& bt, const viss_geometry* geo, const Tuning& tn, float* V,
-                 void* ws, size_t ws_bytes, cudaStream_t st, const viss_fine_map* map = nullptr) {
+                 void* ws, size_t ws_bytes, cudaStream_t st, const viss_fine_map* map = nullptr,
+                 const int32_t* widx = nullptr) {
   VisPlan p;
-  plan_vis(p, cfg, bt, sky.J, geo, tn, map);
+  plan_vis(p, cfg, bt, sky.J, geo, tn, map, widx != nullptr);
   int rc = check_ws(ws, ws_bytes, p.bytes);
   if (rc) return rc;
   if (vis.K == 0) return VISS_OK;
@@ -368,7 +373,7 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
       viss_sky sc = sky;
       if (bt.bright) sc.bright = bt.bright + (int64_t)c * sky.J;
       if ((rc = launch_vis_plain(cfg, sc, channel_rows(vis, r0, r1), geo, p.satdir, dlmn,
-                                 reinterpret_cast<float2*>(V) + r0, st, map, p.flags)))
+                                 reinterpret_cast<float2*>(V) + r0, st, map, p.flags, widx)))
         return rc;
     }
     return VISS_OK;
@@ -383,7 +388,9 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   pa.sl = scale[0]; pa.sm = scale[1]; pa.sn = scale[2]; pa.n_offset = cfg.n_offset;
   pa.res = cfg.res; pa.trunc = map ? 0 : cfg.trunc_brightness;  // the map's base brightness is truncated per member
   pa.rec0 = p.pix0; pa.rec1 = p.pix1; pa.lo = p.plo; pa.geo = p.pgeo; pa.qr = p.pqr;
+  pa.widx = p.ref ? widx : nullptr;
   if ((rc = launch_prep_pixels(pa, st))) return rc;
+  if (p.rrng && (rc = launch_prep_ref_ranges(widx, sky.J, p.Jpad / VIS_P, p.rrng, st))) return rc;
   RowPrepArgs ra{};
   ra.u = vis.u; ra.v = vis.v; ra.w = vis.w; ra.shade = vis.shade;
   ra.snap = p.geo ? vis.snap : nullptr; ra.pair = p.geo ? vis.pair : nullptr;
@@ -413,6 +420,7 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
   vp.mask = cfg.mask_mode;
   vp.ch = bt.ch;
   vp.small_tile = tn.tile & 1;
+  vp.ref_rng = p.rrng;
   if (map) {
     vp.use_map = 1;
     vp.map.box = p.mbox; vp.map.mem = p.mmem; vp.map.members = p.members; vp.map.FF = map->FF;
@@ -675,6 +683,32 @@ int viss_vis_dft_batch(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_
   const float dlmn[3] = {d, d, d};
   return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, bt, geo, make_tuning(tuning), V, workspace, workspace_bytes,
                       static_cast<cudaStream_t>(stream));
+}
+
+size_t viss_vis_dft_windowed_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J) {
+  if (!cfg || K < 0 || J < 0) return 0;
+  Batch bt;
+  if (make_batch(nullptr, K, *cfg, bt)) return 0;
+  VisPlan p;
+  plan_vis(p, *cfg, bt, J, nullptr, Tuning{}, nullptr, true);
+  return p.bytes;
+}
+
+int viss_vis_dft_windowed(const viss_dft_cfg* cfg, const viss_sky* sky, const int32_t* win_index,
+                          const viss_vis_set* vis, float* V, void* workspace, size_t workspace_bytes, void* stream) {
+  int rc;
+  if ((rc = check_vis_call(cfg, sky, vis, nullptr, nullptr, V))) return rc;
+  if (cfg->mask_mode != VISS_MASK_REF_QUIRK && cfg->mask_mode != VISS_MASK_REF_INTENDED)
+    return fail(VISS_ERR_INVALID, "viss_vis_dft_windowed needs a REF mask mode");
+  if (sky->J > 0 && !win_index) return fail(VISS_ERR_INVALID, "win_index is NULL");
+  Batch bt;
+  if ((rc = make_batch(nullptr, vis->K, *cfg, bt))) return rc;
+  const double s = cfg->phase_scale;
+  const double scale[3] = {s, s, s};
+  const float d = (float)(1.0 / s);
+  const float dlmn[3] = {d, d, d};
+  return vis_dft_impl(*cfg, scale, dlmn, *sky, *vis, bt, nullptr, Tuning{}, V, workspace, workspace_bytes,
+                      static_cast<cudaStream_t>(stream), nullptr, win_index);
 }
 
 static int check_map(const viss_fine_map* map, int64_t J) {

@@ -5,6 +5,8 @@
 //
 //   vissGen10M_shade   vissGen10M_shade.cu:178-611 (+ _optim1/_optim2 file names)
 //   vissGen1M_shade    vissGen1M_shade_optim1.cu:265-726 (uvwMap130 weights, NX expansion)
+//   vissGen1M_shade_appro     vissGen1M_shade_appro.cu:153-605 (coarse mean brightness,
+//                      window on NX[j] - 1, d = 2.000955, F_recon_1M_appro/Ex...)
 //   vissGen1M_shade_accurate  vissGen1M_shade_accurate.cu:95-620 (int-truncated
 //                      brightness, F_recon_1M_accu/Ex{p}frequency1M.txt; the reference
 //                      file itself does not compile: `totalnode` is undeclared at :300)
@@ -175,7 +177,8 @@ int vissgen(const Args& a, bool tenM) {
     for (int64_t j = 0; identity && j < J; ++j) identity = cl[j] == 1.0f;
     for (int64_t i = 0; identity && i < X; ++i) identity = (int64_t)NXq[i] == i;
   }
-  for (auto& x : n) x = std::fmax(-1.0f, std::fmin(1.0f, x));  // clip_functor (:308)
+  if (tenM)  // clip_functor (vissGen10M_shade.cu:308); the 1M programs do not clip
+    for (auto& x : n) x = std::fmax(-1.0f, std::fmin(1.0f, x));
 
   std::unordered_map<long long, float> uvwmap;  // 1M: uvwMap130.txt weights
   if (!tenM) {
@@ -343,6 +346,132 @@ int vissgen(const Args& a, bool tenM) {
   return 0;
 }
 
+// ------------------------------------------------------------------ appro
+// vissGen1M_shade_appro.cu:153-605: C_j = mean of FF over the fine pixels with
+// NX == j + 1 (computeC, :72-90; 0 without members), the window of row k tested
+// on NX[j] - 1 (:113-118; the 240 replaces C_j for that term only: the
+// reference's write into the shared C is a race), d = (float)2 * RES / (RES - 1)
+// (:155-157), reconstruction without a mask (its masked value is overwritten,
+// :142-144), uvwMap130 weights, F / K, written expanded to the fine grid as
+// F_recon_1M_appro/Ex{p}frequency1M.txt (:553-568).
+int appro(const Args& a) {
+  const std::string root = a.get("root", ".");
+  const int RES = (int)a.geti("res", 2094);
+  const int start_period = (int)a.geti("start-period", 0);
+  const int days = (int)a.geti("days", 1);
+  const std::string prec_s = a.get("precision", "fast");
+  const int precision = prec_s == "plain" ? VISS_PREC_PLAIN : prec_s == "comp" ? VISS_PREC_COMPENSATED : VISS_PREC_FAST;
+  const std::string mask_s = a.get("mask", "quirk");
+  const int mask = mask_s == "intended" ? VISS_MASK_REF_INTENDED : VISS_MASK_REF_QUIRK;
+  const float d = (float)2 * RES / (RES - 1);
+  const std::string dir = root + "/frequency_1M/";
+  std::vector<float> l, m, n, NX, FF;
+  int64_t J = 0, X = 0;
+  if (read_col(dir + "l.txt", true, l, &J) || read_col(dir + "m.txt", false, m) || read_col(dir + "n.txt", false, n) ||
+      read_col(dir + "NX.txt", false, NX) || read_col(dir + "FF.txt", true, FF, &X)) {
+    std::fprintf(stderr, "cannot read the sky files under %s: %s\n", dir.c_str(), viss_last_error());
+    return 1;
+  }
+  if ((int64_t)l.size() < J || (int64_t)m.size() < J || (int64_t)n.size() < J || (int64_t)FF.size() < X) {
+    std::fprintf(stderr, "sky files shorter than their headers\n");
+    return 1;
+  }
+  l.resize(J); m.resize(J); n.resize(J); FF.resize(X);
+  NX.resize((size_t)X, 0.0f);
+  // computeC: float sums in fine-index order
+  std::vector<float> Csum(J, 0.0f), C(J, 0.0f);
+  std::vector<int> cnt(J, 0);
+  for (int64_t i = 0; i < X; ++i) {
+    const int64_t q = (int64_t)NX[i] - 1;
+    if (q >= 0 && q < J && (float)(q + 1) == NX[i]) { Csum[q] += FF[i]; ++cnt[q]; }
+  }
+  for (int64_t j = 0; j < J; ++j) C[j] = cnt[j] > 0 ? Csum[j] / (float)cnt[j] : 0.0f;
+  std::vector<int32_t> widx(J);
+  for (int64_t j = 0; j < J; ++j) widx[j] = j < X ? (int32_t)NX[j] - 1 : -1;
+  std::unordered_map<long long, float> uvwmap;
+  {
+    int64_t rows = 0;
+    const std::string mp_path = dir + "uvwMap130.txt";
+    if (viss_text_read_floats(mp_path.c_str(), 1, 4, nullptr, 0, &rows, nullptr) == VISS_OK) {
+      std::vector<float> mp((size_t)rows * 4);
+      int64_t hv;
+      viss_text_read_floats(mp_path.c_str(), 1, 4, mp.data(), rows, &rows, &hv);
+      for (int64_t r = 0; r < rows; ++r) {
+        const long long key = ((long long)(int)mp[r] * 1000003LL + (long long)(int)mp[rows + r]) * 1000003LL +
+                              (long long)(int)mp[2 * rows + r];
+        uvwmap[key] = mp[3 * rows + r];
+      }
+    }
+  }
+  Dev<float> dl_, dm_, dn_, dC;
+  Dev<int32_t> dwidx;
+  if (dl_.up(l.data(), J) || dm_.up(m.data(), J) || dn_.up(n.data(), J) || dC.up(C.data(), J) ||
+      dwidx.up(widx.data(), J)) {
+    std::fprintf(stderr, "device allocation failed\n");
+    return 1;
+  }
+  const std::string outdir = root + "/F_recon_1M_appro/";
+  mkdir_p(outdir);
+  for (int p = start_period; p < days; ++p) {
+    std::vector<float> uvw;
+    int64_t K = 0;
+    const std::string uvw_path = dir + "uvw" + std::to_string(p + 1) + "frequency1M.txt";
+    if (read_cols(uvw_path, 3, uvw, &K)) {
+      std::fprintf(stderr, "cannot read %s\n", uvw_path.c_str());
+      return 1;
+    }
+    std::vector<float> wgt(K, 1.0f);
+    for (int64_t k = 0; k < K; ++k) {
+      const long long key = ((long long)(int)uvw[k] * 1000003LL + (long long)(int)uvw[K + k]) * 1000003LL +
+                            (long long)(int)uvw[2 * K + k];
+      auto it = uvwmap.find(key);
+      wgt[k] = it != uvwmap.end() ? 1.0f / it->second : 1.0f;
+    }
+    const std::string sh_path = dir + "shadeM" + std::to_string(p + 1) + "frequency1M.txt";
+    int64_t Ks = 0;
+    std::vector<int32_t> raw;
+    if (viss_text_read_ints(sh_path.c_str(), 4, nullptr, 0, &Ks) == VISS_OK) {
+      raw.resize((size_t)Ks * 4);
+      viss_text_read_ints(sh_path.c_str(), 4, raw.data(), Ks, &Ks);
+    }
+    std::vector<int32_t> sh(4 * (size_t)K, 0);
+    for (int64_t k = 0; k < K && k < Ks; ++k) {
+      const int32_t* r = &raw[4 * k];
+      sh[4 * k] = std::min(r[0], r[1]) - 1; sh[4 * k + 1] = std::max(r[0], r[1]) - 1;
+      sh[4 * k + 2] = std::min(r[2], r[3]) - 1; sh[4 * k + 3] = std::max(r[2], r[3]) - 1;
+    }
+    Dev<float> du, dv, dw, dwgt, dV, dF;
+    Dev<int32_t> dsh;
+    Dev<char> ws;
+    if (du.up(uvw.data(), K) || dv.up(uvw.data() + K, K) || dw.up(uvw.data() + 2 * K, K) || dwgt.up(wgt.data(), K) ||
+        dsh.up(sh.data(), 4 * K) || dV.alloc(2 * K) || dF.alloc(2 * J)) {
+      std::fprintf(stderr, "device allocation failed\n");
+      return 1;
+    }
+    viss_dft_cfg cfg{};
+    cfg.mask_mode = mask; cfg.recon_mask = VISS_RECON_MASK_NONE; cfg.precision = precision; cfg.res = RES;
+    cfg.trunc_brightness = 0; cfg.occluded_value = 240.0f; cfg.phase_scale = 1.0 / (double)d; cfg.n_offset = 0.0;
+    cfg.moon_radius_km = 1737.4; cfg.norm = K > 0 ? 1.0 / (double)K : 1.0;
+    viss_sky sky{dl_.p, dm_.p, dn_.p, dC.p, J};
+    viss_vis_set vs{du.p, dv.p, dw.p, dwgt.p, dsh.p, nullptr, nullptr, K};
+    const size_t nb = std::max(viss_vis_dft_windowed_workspace(&cfg, K, J), viss_recon_workspace(&cfg, K, J, nullptr));
+    if (ws.alloc(nb)) return 1;
+    CHECKV(viss_vis_dft_windowed(&cfg, &sky, dwidx.p, &vs, dV.p, ws.p, nb, nullptr));
+    CHECKV(viss_recon(&cfg, &sky, &vs, nullptr, dV.p, dF.p, ws.p, nb, nullptr));
+    std::vector<float> F(2 * J);
+    CHECKC(cudaMemcpy(F.data(), dF.p, sizeof(float) * 2 * J, cudaMemcpyDeviceToHost));
+    std::vector<float> re(X);
+    for (int64_t c = 0; c < X; ++c) {
+      const int64_t q = (int64_t)NX[c] - 1;
+      re[c] = q >= 0 && q < J ? F[2 * q] : 0.0f;
+    }
+    const std::string out = outdir + "Ex" + std::to_string(p + 1) + "frequency1M.txt";
+    CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
+    std::printf("Period %d: %lld uvw -> %s\n", p + 1, (long long)K, out.c_str());
+  }
+  return 0;
+}
+
 // ------------------------------------------------------------------ shade
 int shade(const Args& a, const std::string& which) {
   const std::string root = a.get("root", ".");
@@ -456,13 +585,15 @@ int main(int argc, char** argv) {
     Args b = a;
     if (prog.find("optim2") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "optim2";
     if (prog.find("accurate") != std::string::npos && !a.kv.count("variant")) b.kv["variant"] = "accurate";
+    if (prog.find("appro") != std::string::npos) return appro(a);
     return vissgen(b, false);
   }
   if (prog == "shade1M" || prog == "shade10M" || prog == "shade30M") return shade(a, prog);
   if (prog.rfind("MIncline", 0) == 0) return mincline(a);
   std::fprintf(stderr,
                "usage: viss_dropin {vissGen10M_shade|vissGen10M_shade_optim1|vissGen10M_shade_optim2|"
-               "vissGen1M_shade_optim1|vissGen1M_shade_optim2|vissGen1M_shade_accurate|shade1M|shade10M|shade30M|"
+               "vissGen1M_shade_optim1|vissGen1M_shade_optim2|vissGen1M_shade_accurate|vissGen1M_shade_appro|"
+               "shade1M|shade10M|shade30M|"
                "MIncline_generate_uvw_float} [--root DIR] [--flag value ...]\n");
   return 2;
 }

@@ -53,8 +53,31 @@ __global__ void prep_pixels_kernel(PixPrepArgs a) {
   }
   if (a.qr) {
     const int res = a.res > 0 ? a.res : 1;
-    a.qr[pos] = make_int2((int)(j / res), (int)(j % res));
+    const int64_t i = a.widx ? (int64_t)a.widx[j] : j;
+    int64_t q = i / res, r = i - q * res;
+    if (r < 0) { r += res; --q; }  // floor division for negative indices
+    a.qr[pos] = make_int2((int)q, (int)r);
   }
+}
+
+// {min, max} of widx over each run of VIS_P positions (the fine indices a vis
+// tile's REF windows test), {1, 0} for a run past J
+__global__ void ref_ranges_kernel(const int32_t* widx, int64_t J, int64_t ntiles, int2* rng) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  int lo = 0x7fffffff, hi = -0x7fffffff - 1;
+  for (int64_t j = t * VIS_P; j < (t + 1) * VIS_P && j < J; ++j) {
+    lo = min(lo, widx[j]);
+    hi = max(hi, widx[j]);
+  }
+  rng[t] = lo <= hi ? make_int2(lo, hi) : make_int2(1, 0);
+}
+
+int launch_prep_ref_ranges(const int32_t* widx, int64_t J, int64_t ntiles, int2* rng, cudaStream_t st) {
+  if (ntiles <= 0) return VISS_OK;
+  ref_ranges_kernel<<<(unsigned)((ntiles + 127) / 128), 128, 0, st>>>(widx, J, ntiles, rng);
+  VISS_LAUNCH_CHECK("ref_ranges_kernel");
+  return VISS_OK;
 }
 
 // ------------------------------------------------------------- pixel order

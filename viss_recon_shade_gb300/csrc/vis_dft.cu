@@ -280,6 +280,10 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP,
               const int2 tr = p.map.tile_rng[tile / VIS_P];
               tlo = tr.x;
               thi = tr.y;
+            } else if (p.ref_rng) {
+              const int2 tr = p.ref_rng[tile / VIS_P];
+              tlo = tr.x;
+              thi = tr.y;
             }
             if (lo_idx <= thi && hi_idx >= tlo) hit = true;
           }
@@ -317,7 +321,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP,
         for (int i = 0; i < VIS_TK; ++i) {
           const int4 wv = sm.win[tid + i * VIS_THREADS];
           const float c = p.use_map ? ref_map_value(p.map, wv, bx, c0, occ_val, tile + pi, p.res)
-                                    : (ref_hit(wv, qr.x, qr.y, tile + pi, p.res) ? occ_val : c0);
+                                    : (ref_hit(wv, qr.x, qr.y, (int64_t)qr.x * p.res + qr.y, p.res) ? occ_val : c0);
           vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
                                tr[i], ti[i]);
         }
@@ -480,6 +484,7 @@ struct PlainVisArgs {
   double R;
   float2* out;
   int* flags;  // near-limb count (may be null)
+  const int32_t* widx;  // REF windows test widx[j] (NULL: j)
   // non-identity fine->coarse map: FF, NXq (float or int), countLoc
   const float* FF;
   const float* NXq_f;
@@ -540,8 +545,10 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
           c = a.occ;
       }
     } else if (wv.x <= wv.y) {
-      const int64_t q = j / a.res, r = j % a.res;
-      if (ref_hit(wv, (int)q, (int)r, j, a.res)) c = a.occ;
+      const int64_t i = a.widx ? (int64_t)a.widx[j] : j;  // the fine index the window tests
+      int64_t q = i / a.res, r = i - q * a.res;
+      if (r < 0) { r += a.res; --q; }
+      if (ref_hit(wv, (int)q, (int)r, i, a.res)) c = a.occ;
     } else if (geo) {
       const float sx = a.l[j], sy = a.m[j], sz = a.n[j];
       if (geo_test_plain(sx, sy, sz, d1, p1, a.R, a.flags) || geo_test_plain(sx, sy, sz, d2, p2, a.R, a.flags))
@@ -560,9 +567,10 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
 
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                      const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
-                     const viss_fine_map* map, int* flags) {
+                     const viss_fine_map* map, int* flags, const int32_t* widx) {
   PlainVisArgs a{};
   a.flags = flags;
+  a.widx = widx;
   if (map) {
     a.FF = map->FF; a.NXq_f = map->NXq_f; a.NXq_i = map->NXq_i; a.countLoc = map->countLoc; a.X = map->X;
   }

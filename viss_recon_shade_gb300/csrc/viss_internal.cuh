@@ -156,7 +156,8 @@ struct PixPrepArgs {
   int4* rec1;     // {x, y, s*n (float bits), j}
   float4* lo;     // {a_lo, b_lo, c_lo, 0}
   float4* geo;    // {unit s, j bits}
-  int2* qr;       // {j / res, j % res}
+  int2* qr;       // {i / res, i % res} of the fine index i the REF windows test
+  const int32_t* widx;  // i = widx[j] (NULL: i = j)
 };
 
 // Visibility rows of a (batched) pass: channel c owns input rows
@@ -255,6 +256,7 @@ struct VisParams {
   // the mean over its fine members, each replaced by the occluded value inside
   // k's window (vissGen10M_shade.cu:120-136)
   FineMapDev map;
+  const int2* ref_rng;    // per VIS_P positions: {min, max} fine index the REF windows test (NULL: the positions)
   int use_map;            // 0: identity map
   int small_tile;         // sky tiles of VIS_P / 2 pixels
 };
@@ -335,7 +337,8 @@ int prep_fine_map(const float* NXq_f, const int32_t* NXq_i, const int32_t* count
 int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out, cudaStream_t st);
 int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vis_set& vis,
                      const viss_geometry* geo, const float4* satdir, const float* dlmn, float2* out, cudaStream_t st,
-                     const viss_fine_map* map = nullptr, int* flags = nullptr);
+                     const viss_fine_map* map = nullptr, int* flags = nullptr, const int32_t* widx = nullptr);
+int launch_prep_ref_ranges(const int32_t* widx, int64_t J, int64_t ntiles, int2* rng, cudaStream_t st);
 
 int launch_recon_fast(const ReconParams& p, int ctas_per_sm, bool compensated, cudaStream_t st);
 int launch_recon_reduce(const RecReduceParams& p, cudaStream_t st);
