@@ -288,11 +288,13 @@ def test_geometric_mask_exact_counts(V, oracle):
 
 
 # ------------------------------------------------------------------ properties at size
-def test_linearity_and_adjoint_large(V):
-    """Full-size properties: linearity of V in the brightness and the adjoint identity
+@pytest.mark.parametrize("workload", ["cfg4_10MHz", "cfg2_10MHz"])
+def test_linearity_and_adjoint_large(V, workload):
+    """Full-size properties (the 10 MHz workloads up to the headline's 1,835,008 x
+    196,608): linearity of V in the brightness and the adjoint identity
     Re<A x, y> = <x, Re(A^H y)> with the geometric mask."""
     from viss_recon_shade_gb300.synth import WORKLOADS, make_sky, make_uvw
-    wl = WORKLOADS["cfg4_10MHz"]
+    wl = WORKLOADS[workload]
     d = make_uvw(wl)
     l, m, n, b = make_sky(wl)
     J = l.size
