@@ -140,11 +140,14 @@ __device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const floa
   // fixed point stays, a 2-cycle ends on the value the parity of the updates
   // left selects.  In FP32 a few percent of samples end in such a cycle without
   // meeting the exit test; they leave at the repeat with the same result.
+  // With e = 0 the first test already sees err = M - (M - 0 * sinf(M)) = 0 and
+  // leaves E0 = M.  The exit test is the reference's double comparison: a float
+  // is below 1e-15 exactly when it is below 1e-15f (no float lies between).
   float E0 = M, Ep = M;
-  for (int i = 1; i < 100; ++i) {
+  for (int i = 1; i < 100 && o.e != 0.f; ++i) {
     const float M0 = E0 - o.e * sinf(E0);
     const float err = M - M0;
-    if (fabsf(err) < 1e-15) break;
+    if (fabsf(err) < 1e-15f) break;
     const float En = E0 + err / (1 - o.e * cosf(E0));
     if (__float_as_int(En) == __float_as_int(E0)) break;
     if (i >= 2 && __float_as_int(En) == __float_as_int(Ep)) {
@@ -156,7 +159,8 @@ __device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const floa
   }
   const float temp = tanf(E0 / 2) / sqrtf((1 - o.e) / (1 + o.e));
   const float theta = atanf(temp) * 2;
-  const float r = o.a * (1 - o.e * o.e) / (1 + o.e * cosf(theta));
+  // e = 0: a * 1 / 1 = a exactly, without evaluating cosf(theta)
+  const float r = o.e != 0.f ? o.a * (1 - o.e * o.e) / (1 + o.e * cosf(theta)) : o.a;
   const float w = theta + o.argp;
   out[0] = r * (cosf(w) * cosf(raan) - sinf(w) * cosf(o.incl) * sinf(raan));
   out[1] = r * (cosf(w) * sinf(raan) + sinf(w) * cosf(o.incl) * cosf(raan));
