@@ -113,3 +113,45 @@ def test_batch_workspace_grows_with_channel_padding(L):
     assert many > single
     r = L.lib.viss_recon_batch_workspace(C.byref(cfg), C.byref(b), 10000, 5000, C.byref(geo), None)
     assert r > 0 and r % 256 == 0
+
+
+def test_stage1_and_window_entry_points_check_arguments(L):
+    """viss_unique_uvw, viss_vis_dft_windowed and viss_workspace_limb_count reject
+    bad arguments on the host; an empty snapshot set is a valid no-op."""
+    dummy = C.c_void_p(16)
+    cnt = C.c_int64(-1)
+    unique = L.lib.viss_unique_uvw
+    assert unique(dummy, 10, 8, 1, 30.0, None, None, None, 0, None, None, 0, None) == L.VISS_ERR_INVALID
+    assert unique(dummy, 10, 1, 1, 30.0, None, None, None, 0, C.byref(cnt), None, 0, None) == L.VISS_ERR_RANGE
+    assert cnt.value == 0
+    assert unique(dummy, 10, 8, 1, 0.0, None, None, None, 0, C.byref(cnt), None, 0, None) == L.VISS_ERR_RANGE
+    assert unique(dummy, 10, 8, 1, float("nan"), None, None, None, 0, C.byref(cnt), None, 0, None) == \
+        L.VISS_ERR_RANGE
+    assert unique(dummy, -1, 8, 1, 30.0, None, None, None, 0, C.byref(cnt), None, 0, None) == L.VISS_ERR_RANGE
+    assert unique(dummy, 10, 8, 1, 30.0, None, None, None, -1, C.byref(cnt), None, 0, None) == L.VISS_ERR_RANGE
+    cnt.value = -1
+    assert unique(None, 0, 8, 1, 30.0, None, None, None, 0, C.byref(cnt), None, 0, None) == L.VISS_OK
+    assert cnt.value == 0
+    assert unique(None, 10, 8, 1, 30.0, None, None, None, 0, C.byref(cnt), None, 0, None) == L.VISS_ERR_INVALID
+    assert unique(dummy, 10, 8, 1, 30.0, None, None, None, 5, C.byref(cnt), None, 0, None) == L.VISS_ERR_INVALID
+    nb = L.lib.viss_unique_uvw_workspace(10, 8, 1)
+    assert nb > 0 and L.lib.viss_unique_uvw_workspace(0, 8, 1) == 0 and L.lib.viss_unique_uvw_workspace(10, 1, 1) == 0
+    assert unique(dummy, 10, 8, 1, 30.0, None, None, None, 0, C.byref(cnt), None, nb, None) == L.VISS_ERR_WORKSPACE
+    assert unique(dummy, 10, 8, 1, 30.0, None, None, None, 0, C.byref(cnt), C.c_void_p(16), nb, None) == \
+        L.VISS_ERR_WORKSPACE  # not 256-byte aligned
+    assert L.lib.viss_unique_uvw_workspace(10, 8, 1) > L.lib.viss_unique_uvw_workspace(10, 8, 0)
+
+    cfg = L.DftCfg(1, 0, 1, 8, 0, 240.0, 0.5, 0.0, 1737.4, 1.0)  # REF_QUIRK, res 8
+    sky = L.Sky(dummy, dummy, dummy, dummy, 3)
+    vis = L.VisSet(dummy, dummy, dummy, None, None, None, None, 5)
+    win = L.lib.viss_vis_dft_windowed
+    assert win(C.byref(cfg), C.byref(sky), dummy, C.byref(vis), dummy, None, 0, None) == L.VISS_ERR_INVALID
+    assert b"shade windows" in L.lib.viss_last_error()
+    vis.shade = dummy
+    assert win(C.byref(cfg), C.byref(sky), None, C.byref(vis), dummy, None, 0, None) == L.VISS_ERR_INVALID
+    assert b"win_index" in L.lib.viss_last_error()
+    cfg.mask_mode = 0
+    assert win(C.byref(cfg), C.byref(sky), dummy, C.byref(vis), dummy, None, 0, None) == L.VISS_ERR_INVALID
+    assert b"REF mask" in L.lib.viss_last_error()
+    assert L.lib.viss_workspace_limb_count(None, C.byref(cnt), None) == L.VISS_ERR_INVALID
+    assert L.lib.viss_workspace_limb_count(dummy, None, None) == L.VISS_ERR_INVALID
