@@ -18,26 +18,29 @@
 
 namespace viss {
 
-// x / d for 0 <= x < 2^62 by a multiply-high with magic = ceil(2^64 / d),
-// corrected by one step either way
+// x / d for 0 <= x < 2^31 by a multiply-high with magic = ceil(2^32 / d)
+// (the estimate is floor(x / d) or one above it), corrected by one step either way
 struct FastDiv {
-  int64_t d = 1;
-  uint64_t magic = 0;
-  void set(int64_t dd) { d = dd; magic = dd > 1 ? ~0ull / (uint64_t)dd + 1 : 0; }
-  __device__ __forceinline__ int64_t div(int64_t x) const {
+  int d = 1;
+  uint32_t magic = 0;
+  void set(int dd) { d = dd; magic = dd > 1 ? 0xFFFFFFFFu / (uint32_t)dd + 1 : 0; }
+  __device__ __forceinline__ int div(int x) const {
     if (d == 1) return x;
-    int64_t q = (int64_t)__umul64hi((uint64_t)x, magic);
-    const int64_t r = x - q * d;
+    int q = (int)__umulhi((uint32_t)x, magic);
+    const int r = x - q * d;
     if (r < 0) --q;
     else if (r >= d) ++q;
     return q;
   }
 };
 
+// Every index below is a 32-bit int: the launcher admits only
+// orbit_res * orbit_counts * (nsat + 1) < 2^31 (the reference's own int indices),
+// so sample indices, snapshots, threads and 3 x threads all stay below 2^31.
 struct OrbitDev {
   int nsat, orbit_res, orbit_counts, index;
   int span, interval;
-  int64_t total, S, half, reset_index;
+  int total, S, half, reset_index;
   FastDiv by_span, by_res, by_nsat;
   float a, e, incl, argp, d2r;
   double dm_den;                 // (double)(2a) * 1e3, the divisor of calculate_dM
@@ -54,17 +57,17 @@ struct OrbitDev {
 // read of one element past the satellite's array (kind 2): that is the next
 // satellite's slot, not yet computed when uvwPosition runs for this satellite
 // (:224-308), so it reads zero as well.
-__device__ __forceinline__ int window_index(const OrbitDev& o, int64_t g, int64_t* circle) {
-  const int64_t k = o.by_span.div(g) + 1;
-  const int64_t offset = (k - 1) * o.interval;
-  int64_t endIdx = (k - 1) * o.orbit_res + offset + o.span;
-  int64_t startIdx = (k - 1) * o.orbit_res + offset;
-  if ((k - 1) * (int64_t)(o.orbit_res + o.interval) > o.total) {
-    const int64_t reset_index = o.reset_index;  // total / (orbit_res + interval) + 1
+__device__ __forceinline__ int window_index(const OrbitDev& o, int g, int* circle) {
+  const int k = o.by_span.div(g) + 1;
+  const int offset = (k - 1) * o.interval;
+  int endIdx = (k - 1) * o.orbit_res + offset + o.span;
+  int startIdx = (k - 1) * o.orbit_res + offset;
+  if ((k - 1) * (o.orbit_res + o.interval) > o.total) {
+    const int reset_index = o.reset_index;  // total / (orbit_res + interval) + 1
     startIdx = (k - 1 - reset_index) * o.orbit_res + offset;
     endIdx = (k - 1 - reset_index) * o.orbit_res + offset + o.span;
   }
-  const int64_t c = startIdx + (g - (k - 1) * o.span);
+  const int c = startIdx + (g - (k - 1) * o.span);
   *circle = c;
   if (endIdx > o.total) {
     if (c > o.total) return 1;
@@ -121,11 +124,10 @@ constexpr int RAAN_TAB = 4;  // orbits per block with a precomputed RAAN
 // reference's expression shape: written with cosf/sinf values computed elsewhere
 // the compiler fuses its products differently, and about half of the positions
 // move by an ulp.
-__device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const float* raan_tab, int k_base,
+__device__ void position_f32(const OrbitDev& o, int sat, int idx, const float* raan_tab, int k_base,
                              float* out) {
-  const int64_t half = o.half;
-  const int64_t kq = o.by_res.div(idx);
-  const int k = (int)kq, po = (int)(idx - kq * o.orbit_res);
+  const int half = o.half;
+  const int k = o.by_res.div(idx), po = idx - k * o.orbit_res;
   float d;
   if (idx < half) d = fmaf(o.s1[sat], (float)idx, o.r1[sat]);   // linspace r1 -> r2 (:42-49)
   else d = fmaf(o.s2[sat], (float)(idx - half), o.r2[sat]);     // linspace r2 -> r1
@@ -157,7 +159,9 @@ __device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const floa
     Ep = E0;
     E0 = En;
   }
-  const float temp = tanf(E0 / 2) / sqrtf((1 - o.e) / (1 + o.e));
+  // e = 0: the divisor is sqrtf(1 / 1) = 1 and the quotient tanf(E0 / 2) itself
+  const float tan_half = tanf(E0 / 2);
+  const float temp = o.e != 0.f ? tan_half / sqrtf((1 - o.e) / (1 + o.e)) : tan_half;
   const float theta = atanf(temp) * 2;
   // e = 0: a * 1 / 1 = a exactly, without evaluating cosf(theta)
   const float r = o.e != 0.f ? o.a * (1 - o.e * o.e) / (1 + o.e * cosf(theta)) : o.a;
@@ -167,9 +171,9 @@ __device__ void position_f32(const OrbitDev& o, int sat, int64_t idx, const floa
   out[2] = r * (sinf(w) * sinf(o.incl));
 }
 
-__device__ void position_f64(const OrbitDev& o, int sat, int64_t idx, double* out) {
-  const int64_t half = o.total / 2;
-  const int64_t k = idx / o.orbit_res, po = idx % o.orbit_res;
+__device__ void position_f64(const OrbitDev& o, int sat, int idx, double* out) {
+  const int half = o.total / 2;
+  const int k = idx / o.orbit_res, po = idx % o.orbit_res;
   const double d2r = kPi / 180.0;
   const double r1 = o.r1[sat], r2 = o.r2[sat];
   double d;
@@ -205,18 +209,18 @@ __global__ void orbit_positions_kernel(const OrbitDev o, float* pos, double* pos
   __shared__ float raan_tab[RAAN_TAB];
   __shared__ int k_base_s;
   if (!o.fp64 && threadIdx.x < RAAN_TAB) {
-    int64_t c0;
-    const int kind0 = window_index(o, o.by_nsat.div((int64_t)blockIdx.x * blockDim.x), &c0);
-    const int k0 = kind0 == 0 ? (int)o.by_res.div(c0) : 0;
+    int c0;
+    const int kind0 = window_index(o, o.by_nsat.div((int)(blockIdx.x * blockDim.x)), &c0);
+    const int k0 = kind0 == 0 ? o.by_res.div(c0) : 0;
     raan_tab[threadIdx.x] = raan_of(k0 + (int)threadIdx.x, (o.index - 1) * o.orbit_counts, o.d2r, o.raan_step);
     if (threadIdx.x == 0) k_base_s = k0;
   }
   __syncthreads();
-  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
   if (t >= o.S * o.nsat) return;
-  const int64_t g = o.by_nsat.div(t);
-  const int sat = (int)(t - g * o.nsat);
-  int64_t circle;
+  const int g = o.by_nsat.div(t);
+  const int sat = t - g * o.nsat;
+  int circle;
   const int kind = window_index(o, g, &circle);
   const bool zero = kind != 0;
   if (o.fp64) {
@@ -678,8 +682,8 @@ int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, v
   o.nsat = cfg->nsat; o.orbit_res = cfg->orbit_res; o.orbit_counts = cfg->orbit_counts; o.index = cfg->index;
   o.span = cfg->orbit_res / 3;
   o.interval = cfg->orbit_res / 360 * 10;
-  o.total = (int64_t)cfg->orbit_res * cfg->orbit_counts;
-  o.S = (int64_t)cfg->orbit_counts * o.span;
+  o.total = cfg->orbit_res * cfg->orbit_counts;  // below 2^31 by the check above
+  o.S = cfg->orbit_counts * o.span;
   o.half = o.total / 2;
   o.reset_index = o.total / (o.orbit_res + o.interval) + 1;
   o.by_span.set(o.span);
@@ -697,7 +701,7 @@ int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, v
   o.raan_step = cfg->raan_step_deg;
   o.step_mt = (float)(2 * kPi) / float(cfg->orbit_res - 1);
   o.fp64 = cfg->fp64;
-  const int64_t half = o.total / 2;
+  const int half = o.total / 2;
   if (half < 2) return fail(VISS_ERR_RANGE, "orbit too short");
   for (int s = 0; s < o.nsat; ++s) {
     o.r1[s] = cfg->r1_m[s];
@@ -705,7 +709,7 @@ int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, v
     o.s1[s] = (o.r2[s] - o.r1[s]) / float(half - 1);
     o.s2[s] = (o.r1[s] - o.r2[s]) / float(half - 1);
   }
-  const int64_t n = o.S * o.nsat;
+  const int64_t n = (int64_t)o.S * o.nsat;
   if (n == 0) return VISS_OK;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   orbit_positions_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(o, pos, pos64);
