@@ -409,7 +409,9 @@ def cpu_baseline(args, wl, d, Vout, Fout, cfg):
             "sample": f"FP64 oracle: {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities "
                       f"({terms:.3g} terms, {dt:.1f} s)",
             "gpu_rel_err_on_sample": {"vis_rms": float(ev), "vis_max": float(evm), "recon_rms": float(ef),
-                                      "recon_max": float(efm)}}
+                                      "recon_max": float(efm),
+                                      "definitions": {"rms": "||gpu - fp64|| / ||fp64|| over the sample",
+                                                      "max": "max |gpu - fp64| / max |fp64| over the sample"}}}
 
 
 # ------------------------------------------------------------------ reference arm
