@@ -414,6 +414,7 @@ __global__ void dedup_hash_kernel(const float* u, const float* v, const float* w
 // equal key there has the smaller row index already.  Baselines move by far
 // less than a wavelength between snapshots, so most rows touch no table slot.
 constexpr int UNIQUE_RUN = 256;
+constexpr int UNIQUE_BATCH = 2;
 
 // Key fields of row (m, n) and row (n, m) for one coordinate: F = ceil(q) + 2^20
 // with q = (double)(+-diff) * 1e3 / lambda, the integers baseline_coord gives
@@ -493,18 +494,22 @@ __global__ void __launch_bounds__(256, 6) unique_insert_kernel(const float* __re
     row_keys(dp, lambda, scale, ordered, &prevf, &prevr, &oor);
   }
   uint32_t rowf = (uint32_t)(qf * S + g0), rowr = (uint32_t)(qr * S + g0);
-  for (int j0 = 0; j0 < cnt; j0 += 4) {
+  // UNIQUE_BATCH snapshots' positions are loaded together.  The kernel runs at
+  // 6 CTAs per SM (40 registers; 4 CTAs without spills measured 11% slower): a
+  // batch of 4 spilled ~1.5x as much and took 10.2 ms on the MIncline campaign
+  // against 9.8 ms for 1 or 2.
+  for (int j0 = 0; j0 < cnt; j0 += UNIQUE_BATCH) {
     const float* ahead = pn + (j0 + 32) * stride;
     if (ahead < pend) asm volatile("prefetch.global.L2 [%0];" ::"l"(ahead));
-    float d[4][3];
+    float d[UNIQUE_BATCH][3];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < UNIQUE_BATCH; ++j) {
       const int o = (j0 + j < cnt ? j0 + j : cnt - 1) * stride;
 #pragma unroll
       for (int c = 0; c < 3; ++c) d[j][c] = __ldg(pn + o + c) - __ldg(pm + o + c);
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < UNIQUE_BATCH; ++j) {
       if (j0 + j >= cnt) break;
       uint64_t kf, kr;
       row_keys(d[j], lambda, scale, ordered, &kf, &kr, &oor);
