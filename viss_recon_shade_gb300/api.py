@@ -231,6 +231,7 @@ class Tuning:
     vis_split: int = 0
     rec_items: int = 0
     tile: int = 0  # bit 0: vis sky tiles of 256 pixels; bit 1 / bit 2: recon row tiles of 128 / 512 rows
+    # (neither: 512 rows where the recon segments average >= 8192 rows, else 256)
 
     def c(self) -> L.Tuning:
         return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), int(self.tile))
