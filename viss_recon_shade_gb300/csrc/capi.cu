@@ -79,7 +79,7 @@ static Tuning make_tuning(const viss_tuning* t) {
     r.ctas_per_sm = t->ctas_per_sm > 0 ? t->ctas_per_sm : 0;
     r.vis_split = t->vis_split > 0 ? t->vis_split : 0;
     r.rec_items = t->rec_items > 0 ? t->rec_items : 0;
-    r.tile = t->tile & 7;
+    r.tile = t->tile & 15;
   }
   return r;
 }
@@ -528,6 +528,7 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   // with 256), 256 for short segments, whose ragged last tile would cost more.
   if ((tn.tile >> 1) & 1) rp.row_tile = 1;
   else if ((tn.tile >> 2) & 1) rp.row_tile = 2;
+  else if ((tn.tile >> 3) & 1) rp.row_tile = 0;
   else rp.row_tile = (p.nseg > 0 && p.K / p.nseg >= 32 * (int64_t)REC_Q) ? 2 : 0;
   rp.npb = (int)p.npb;
   rp.nseg = p.nseg;
