@@ -244,9 +244,8 @@ typedef struct viss_tuning {
   int32_t vis_split;         /* sky chunks per visibility block, each a work item (0: enough for ~32 items per CTA) */
   int32_t rec_items;         /* recon work items per persistent CTA the row segments aim at (0: 64) */
   int32_t tile;              /* tile shapes: bit 0 vis sky tiles of 256 pixels (else 512),
-                                bit 1 recon row tiles of 128 visibilities, bit 2 of 512, bit 3 of
-                                256; none of bits 1-3: 512 where the recon segments average
-                                >= 8192 rows, else 256 */
+                                bit 1 recon row tiles of 128 visibilities, bit 3 of 256
+                                (else 512; bit 2 asks for 512 explicitly) */
 } viss_tuning;
 
 VISS_API size_t viss_vis_dft_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,

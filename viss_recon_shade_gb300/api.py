@@ -230,8 +230,8 @@ class Tuning:
     ctas_per_sm: int = 0
     vis_split: int = 0
     rec_items: int = 0
-    tile: int = 0  # bit 0: vis sky tiles of 256 pixels; bit 1 / 2 / 3: recon row tiles of 128 / 512 / 256
-    # rows (none of them: 512 rows where the recon segments average >= 8192 rows, else 256)
+    tile: int = 0  # bit 0: vis sky tiles of 256 pixels (else 512); bit 1 / 3: recon row tiles of 128 / 256
+    # rows (else 512; bit 2 asks for 512 explicitly)
 
     def c(self) -> L.Tuning:
         return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), int(self.tile))
@@ -338,7 +338,7 @@ def tuning_candidates() -> list:
     """Launch choices the autotuner times: tile shapes (sky tile of the vis kernel, row tile
     of the recon kernel), persistent CTAs per SM, recon items per CTA, sky split."""
     out = []
-    for tile in (0, 1, 2, 3, 4, 5, 8, 9):
+    for tile in (0, 1, 2, 3, 8, 9):
         for items in (16, 32):
             out.append(Tuning(tile=tile, rec_items=items))
     out.append(Tuning(rec_items=8))
