@@ -155,3 +155,21 @@ def test_stage1_and_window_entry_points_check_arguments(L):
     assert b"REF mask" in L.lib.viss_last_error()
     assert L.lib.viss_workspace_limb_count(None, C.byref(cnt), None) == L.VISS_ERR_INVALID
     assert L.lib.viss_workspace_limb_count(dummy, None, None) == L.VISS_ERR_INVALID
+
+
+def test_vis_split_beyond_int_work_items_is_refused(L):
+    """A caller's vis_split that would make more than 2^31 - 1 work items (visibility
+    blocks x sky chunks) is refused on the host, before the workspace is looked at."""
+    dummy = C.c_void_p(16)
+    cfg = L.DftCfg(0, 0, 1, 0, 0, 0.0, 1.0, -1.0, 1737.4, 1.0)  # no mask, FAST
+    sky = L.Sky(dummy, dummy, dummy, dummy, 1 << 30)
+    vis = L.VisSet(dummy, dummy, dummy, None, None, None, None, 1 << 31)
+    t = L.Tuning(0, 1 << 21, 0, 0)  # 2^21 sky chunks x 2^21 visibility blocks
+    rc = L.lib.viss_vis_dft_batch(C.byref(cfg), C.byref(sky), C.byref(vis), None, None, C.byref(t), dummy, None, 0,
+                                  None)
+    assert rc == L.VISS_ERR_RANGE
+    assert b"vis_split" in L.lib.viss_last_error()
+    t.vis_split = 4  # a sane split reaches the workspace check instead
+    rc = L.lib.viss_vis_dft_batch(C.byref(cfg), C.byref(sky), C.byref(vis), None, None, C.byref(t), dummy, None, 0,
+                                  None)
+    assert rc == L.VISS_ERR_WORKSPACE

@@ -355,6 +355,9 @@ int vis_dft_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlm
                  const int32_t* widx = nullptr) {
   VisPlan p;
   plan_vis(p, cfg, bt, sky.J, geo, tn, map, widx != nullptr);
+  // work items are counted in int (a caller's vis_split can ask for more)
+  if (!p.plain && p.nrb * (int64_t)p.nsplit > (int64_t)INT32_MAX)
+    return fail(VISS_ERR_RANGE, "visibility blocks x sky chunks must be < 2^31: lower vis_split");
   int rc = check_ws(ws, ws_bytes, p.bytes);
   if (rc) return rc;
   if (vis.K == 0) return VISS_OK;
