@@ -85,6 +85,21 @@ def _dev(t: Optional[torch.Tensor], dtype, name: str, n: Optional[int] = None, c
     return t
 
 
+def _need(t, dtype, name: str, n: Optional[int] = None) -> torch.Tensor:
+    """A required tensor argument: as _dev, and None is refused."""
+    if t is None:
+        raise TypeError(f"{name} is required")
+    return _dev(t, dtype, name, n)
+
+
+def _positions(pos: torch.Tensor, dtype=torch.float32, name: str = "pos") -> torch.Tensor:
+    """Satellite positions [S, nsat, 3] on the GPU, contiguous."""
+    pos = _need(pos, dtype, name)
+    if pos.dim() != 3 or pos.shape[2] != 3:
+        raise ValueError(f"{name} must be [S, nsat, 3], got {list(pos.shape)}")
+    return pos
+
+
 def _stream():
     return C.c_void_p(torch.cuda.current_stream().cuda_stream)
 
@@ -472,6 +487,8 @@ class OrbitConfig:
 def orbit_positions(cfg: OrbitConfig, device="cuda", want_f64: bool = False):
     """Satellite positions [S, nsat, 3] (km) at the windowed snapshots; with want_f64 also the
     double positions."""
+    if torch.device(device).type != "cuda":
+        raise TypeError("orbit_positions computes on a CUDA device")
     c = cfg.c()
     S = L.lib.viss_orbit_snapshots(C.byref(c))
     pos = torch.empty(S, cfg.nsat, 3, dtype=torch.float32, device=device)
@@ -483,6 +500,10 @@ def orbit_positions(cfg: OrbitConfig, device="cuda", want_f64: bool = False):
 def baseline_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, rounding: bool = True,
                  pos64: Optional[torch.Tensor] = None):
     """uvw per (snapshot, pair), snapshot-major; returns u, v, w, snap, pair."""
+    pos = _positions(pos)
+    pos64 = None if pos64 is None else _positions(pos64, torch.float64, "pos64")
+    if pos64 is not None and pos64.shape != pos.shape:
+        raise ValueError("pos64 must have the shape of pos")
     S, nsat = pos.shape[0], pos.shape[1]
     P = nsat * (nsat - 1) // (1 if ordered else 2)
     K = S * P
@@ -490,7 +511,7 @@ def baseline_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, round
     u, v, w = (torch.empty(K, dtype=torch.float32, device=dev) for _ in range(3))
     snap = torch.empty(K, dtype=torch.int32, device=dev)
     pair = torch.empty(K, dtype=torch.int32, device=dev)
-    L.check(L.lib.viss_baseline_uvw(_ptr(pos.contiguous()), _ptr(pos64), S, nsat, int(ordered), float(lambda_m),
+    L.check(L.lib.viss_baseline_uvw(_ptr(pos), _ptr(pos64), S, nsat, int(ordered), float(lambda_m),
                                     int(rounding), _ptr(u), _ptr(v), _ptr(w), _ptr(snap), _ptr(pair), _stream()),
             "viss_baseline_uvw")
     return u, v, w, snap, pair
@@ -498,8 +519,8 @@ def baseline_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, round
 
 def dedup_uvw(u: torch.Tensor, v: torch.Tensor, w: torch.Tensor):
     """Sort + unique of integer-valued uvw (copies); returns (u, v, w) of the unique count."""
-    u, v, w = (x.clone().contiguous() for x in (u, v, w))
-    K = u.numel()
+    K = u.numel() if isinstance(u, torch.Tensor) else 0
+    u, v, w = (_need(x, torch.float32, nm, K).clone() for x, nm in ((u, "u"), (v, "v"), (w, "w")))
     nb = L.lib.viss_dedup_uvw_workspace(K)
     ws = _workspace(nb, u.device)
     cnt = C.c_int64(0)
@@ -515,7 +536,7 @@ def unique_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, capacit
     occurrence in pair-major order (the reference's concatenation of per-pair lists).  Starts
     with room for `capacity` rows and repeats the pass once with the exact count if that
     is short."""
-    pos = pos.contiguous()
+    pos = _positions(pos)
     S, nsat = pos.shape[0], pos.shape[1]
     nb = L.lib.viss_unique_uvw_workspace(S, nsat, int(ordered))
     ws = _workspace(nb, pos.device)
@@ -535,12 +556,13 @@ def unique_uvw(pos: torch.Tensor, lambda_m: float, ordered: bool = True, capacit
 
 def shade_windows(u, v, w, RES: int, mean_r_km: float = 0.0):
     """Raw shadeM windows int32[K, 4] (1-based) and the mean radius used."""
-    K = u.numel()
+    K = u.numel() if isinstance(u, torch.Tensor) else 0
+    u, v, w = (_need(x, torch.float32, nm, K) for x, nm in ((u, "u"), (v, "v"), (w, "w")))
     out = torch.empty(K, 4, dtype=torch.int32, device=u.device)
     nb = L.lib.viss_shade_windows_workspace(K)
     ws = _workspace(nb, u.device)
     mr = C.c_double(0.0)
-    L.check(L.lib.viss_shade_windows(_ptr(u.contiguous()), _ptr(v.contiguous()), _ptr(w.contiguous()), K, int(RES),
+    L.check(L.lib.viss_shade_windows(_ptr(u), _ptr(v), _ptr(w), K, int(RES),
                                      float(mean_r_km), _ptr(out), C.byref(mr), _ptr(ws), nb, _stream()),
             "viss_shade_windows")
     return out, mr.value
