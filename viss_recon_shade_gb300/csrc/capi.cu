@@ -48,7 +48,7 @@ struct Tuning {
   int ctas_per_sm = 0;
   int vis_split = 0;
   int rec_items = 0;
-  int tile = 0;  // bit 0: vis sky tiles of VIS_P / 2; bit 1: recon row tiles of REC_Q / 2
+  int tile = 0;  // bit 0: vis sky tiles of VIS_P / 2; recon row tiles: bit 1 REC_Q / 2, bit 3 REC_Q, else 2 REC_Q
 };
 
 static int make_batch(const viss_batch* b, int64_t K, const viss_dft_cfg& cfg, Batch& out) {

@@ -5,7 +5,8 @@
 //
 // A work item is REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates
 // in registers) against one segment of visibility rows of one channel, streamed
-// through shared memory in tiles of REC_Q (or REC_Q / 2) rows.  The phase of y_k is folded into the
+// through shared memory in tiles of 2 REC_Q rows (REC_Q or REC_Q / 2 on request).
+// The phase of y_k is folded into the
 // row's fixed-point bias (y e^{ix} = |y| e^{i(x + arg y)}), so a term is the
 // same as in the vis kernel: 3 IMAD [+3 FFMA fractional uvw] [+3 FFMA
 // compensated], turns -> angle, __sincosf, 2 FFMA with |y_k|.
@@ -351,7 +352,7 @@ static void launch_tile(const ReconParams& p, int ctas_per_sm, cudaStream_t st) 
   recon_fast_kernel<RM, COMP, Q><<<g, REC_THREADS, 0, st>>>(p);
 }
 
-// Row tiles of REC_Q visibilities, REC_Q / 2 or 2 REC_Q (tuning).
+// Row tiles of 2 REC_Q visibilities (the default), REC_Q or REC_Q / 2 (tuning).
 template <int RM>
 static void launch_rm(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
   if (p.row_tile == 1) {
