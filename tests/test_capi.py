@@ -22,6 +22,11 @@ def test_exports_every_declared_symbol(L):
     assert set(declared) <= exported
 
 
+def test_every_declared_symbol_has_a_ctypes_signature(L):
+    # a symbol without argtypes would pass 64-bit and double arguments as C int
+    assert set(L.declared_symbols()) == set(L._SIGS)
+
+
 def test_status_strings(L):
     for s in (0, -1, -2, -3, -4, -5, -6, -7, -8):
         assert L.lib.viss_status_str(s)
