@@ -172,8 +172,8 @@ typedef struct viss_fine_map {
   int64_t X;                 /* fine pixels (entries of FF and NXq) */
 } viss_fine_map;
 
-/* Shaded visibility DFT over a fine->coarse map; sky->bright is unused (the
- * coarse brightness comes from FF).  Same configuration and result layout as
+/* Shaded visibility DFT over a fine->coarse map (visscal with NXq/countLoc,
+ * vissGen10M_shade.cu:120-136); sky->bright is unused (the coarse brightness comes from FF).  Same configuration and result layout as
  * viss_vis_dft. */
 VISS_API size_t viss_vis_dft_map_workspace(const viss_dft_cfg* cfg, int64_t K, int64_t J, const viss_fine_map* map,
                                            const viss_geometry* geo);
@@ -208,7 +208,8 @@ VISS_API int viss_vis_dft_windowed(const viss_dft_cfg* cfg, const viss_sky* sky,
  * the reference's form, 8 = a fine-map index outside [0, X) (that pixel is NaN).
  * No counterpart in the reference, which reads such inputs unchecked. */
 VISS_API int viss_workspace_flags(const void* workspace, int32_t* flags, void* stream);
-/* GEOMETRIC mask: how many occlusion tests of the completed pass fell within 2e-6 (in the
+/* No counterpart in the reference (its masks are the REF windows of shade1M.cu:73-105).
+ * GEOMETRIC mask: how many occlusion tests of the completed pass fell within 2e-6 (in the
  * cosine of the angle to the limb) of the Moon's limb and were decided in double from the
  * original inputs instead (count of (visibility, pixel, satellite) tests; the fast kernels
  * test fewer terms than the plain ones, as they drop blocks the cones decide).  Reads the
@@ -298,10 +299,11 @@ typedef struct viss_orbit_cfg {  /* MIncline_generate_uvw_float.cu:22-30, 184-19
 
 /* Number of windowed snapshots: orbit_counts * (orbit_res / 3). */
 VISS_API int64_t viss_orbit_snapshots(const viss_orbit_cfg* cfg);
-/* Satellite positions at every snapshot (calculateOrbit + uvwPosition, :83-151):
+/* Satellite positions at every snapshot (calculateOrbit + uvwPosition,
+ * MIncline_generate_uvw_float.cu:83-151):
  * pos: S x nsat x 3 float (km); pos64 (optional, may be NULL): the same in double. */
 VISS_API int viss_orbit_positions(const viss_orbit_cfg* cfg, float* pos, double* pos64, void* stream);
-/* Baseline uvw (computeUVW, :153-160), snapshot-major then pair.  pairs: 1 = ordered
+/* Baseline uvw (computeUVW, MIncline_generate_uvw_float.cu:153-160), snapshot-major then pair.  pairs: 1 = ordered
  * (m != n, the reference's 56 for 8 satellites), 0 = unordered (m < n).  rounding: 1 = the
  * reference's ceil(), 0 = none.  From pos64 when given (no rounding to float first).
  * snap/pair outputs may be NULL.  K = S * npairs entries are written. */
@@ -309,7 +311,7 @@ VISS_API int viss_baseline_uvw(const float* pos, const double* pos64, int64_t S,
                       double lambda_m, int rounding, float* u, float* v, float* w, int32_t* snap,
                       int32_t* pair, void* stream);
 /* Global lexicographic sort + unique of integer-valued uvw (the reference's per-pair and
- * global thrust sort/unique, :370-397).  In place on u, v, w; *count_out (HOST) receives
+ * global thrust sort/unique, MIncline_generate_uvw_float.cu:370-397).  In place on u, v, w; *count_out (HOST) receives
  * the unique count (the call synchronises the stream).  |u|,|v|,|w| must be < 2^20. */
 VISS_API size_t viss_dedup_uvw_workspace(int64_t K);
 VISS_API int viss_dedup_uvw(float* u, float* v, float* w, int64_t K, int64_t* count_out, void* workspace,
