@@ -176,17 +176,29 @@ def load_workload(name, device="cuda"):
     return wl, d
 
 
-def choose_precision(d, pref):
-    import viss_recon_shade_gb300 as V
+def precision_name(d, pref) -> str:
+    """'fast' or 'compensated' for this workload's uvw (tensors or arrays)."""
     if pref == "fast":
-        return V.PREC_FAST
+        return "fast"
     if pref == "comp":
-        return V.PREC_COMPENSATED
-    umax = max(float(d[k].abs().max()) for k in ("u", "v", "w"))
+        return "compensated"
+    umax = max(float(abs(d[k]).max()) for k in ("u", "v", "w"))
     # the fast path's phase error grows as |uvw| * 2^-33 turns per coordinate; up to
     # |uvw| ~ 1.2e4 (30 MHz, 100 km baselines) it measures <= 1e-5 against FP64
     # (tests/test_gpu_precision.py), beyond that the compensated path is needed
-    return V.PREC_FAST if umax <= 12000 else V.PREC_COMPENSATED
+    return "fast" if umax <= 12000 else "compensated"
+
+
+def choose_precision(d, pref):
+    import viss_recon_shade_gb300 as V
+    return {"fast": V.PREC_FAST, "compensated": V.PREC_COMPENSATED}[precision_name(d, pref)]
+
+
+def workload_config(wl, K, J, precision, ws):
+    """The `config` of both arms' lines (same workload, same keys and values)."""
+    return {"workload": wl.name, "K": K, "J": J, "terms_per_step": int(2 * K * J), "snapshots": wl.snapshots,
+            "baselines": wl.npairs, "freq_hz": wl.freq_hz, "mask": "geometric", "precision": precision,
+            "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}"}
 
 
 def run_ours(args, ws, rank, local):
@@ -336,15 +348,11 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, wl, d, Vout, Fout, cfg)
 
-    names = {V.PREC_FAST: "fast", V.PREC_COMPENSATED: "compensated"}
     line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fixed-point i32 phase)",
             "data": "synthetic (seeded orbit + Fibonacci sky)",
-            "config": {"workload": wl.name, "K": K, "J": J, "terms_per_step": int(terms_step),
-                       "snapshots": wl.snapshots, "baselines": wl.npairs, "freq_hz": wl.freq_hz,
-                       "mask": "geometric", "precision": names.get(prec, str(prec)),
-                       "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}"},
+            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws),
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
@@ -388,8 +396,9 @@ def cpu_baseline(args, wl, d, Vout, Fout, cfg):
     O.vis_dft(ocfg, u[rows], v[rows], w[rows], l, m, n, b, geo=geo_s, nthreads=thr)
     rate = rows.size * J / (time.perf_counter() - t0)
     target_terms = rate * args.cpu_seconds
-    nr = int(min(K, max(64, target_terms / 2 / J)))
-    np_ = int(min(J, max(16, target_terms / 2 / K)))
+    whole = lambda x, cap: int(min(cap, max(thr, round(x / thr) * thr)))  # noqa: E731  (equal shares a thread)
+    nr = whole(target_terms / 2 / J, K)
+    np_ = whole(target_terms / 2 / K, J)
     ridx = np.linspace(0, K - 1, nr).astype(np.int64)
     pidx = np.linspace(0, J - 1, np_).astype(np.int64)
     t0 = time.perf_counter()
@@ -415,29 +424,69 @@ def cpu_baseline(args, wl, d, Vout, Fout, cfg):
 
 
 # ------------------------------------------------------------------ reference arm
+def _synth_standalone():
+    """synth.py loaded by path: the reference arm must not load the product library
+    (importing the package would)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("viss_synth_standalone",
+                                                  ROOT / "viss_recon_shade_gb300" / "synth.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = mod  # dataclasses look their module up
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def reference_workload(name):
+    """The workload's inputs built on the host without the product: satellite
+    positions and continuous uvw from the oracle's FP64 restatement of calculateOrbit /
+    uvwPosition / computeUVW, the sky from numpy.  Same shapes and generators as the
+    product arm's (the last bits of a few uvw may differ: host vs device FP64 sin/cos)."""
+    import numpy as np
+    from oracle import oracle as O
+    S = _synth_standalone()
+    wl = S.WORKLOADS[name]
+    r1, r2 = S.log_separations(wl.nsat)
+    oc = O.make_orbit_cfg(wl.nsat, wl.orbit_res, wl.orbit_counts, index=1, a_km=wl.a_km, incl_deg=wl.incl_deg,
+                          r1_m=r1, r2_m=r2)
+    pos64 = O.orbit_positions_f64(oc, nthreads=O.max_threads())
+    u, v, w = O.uvw_f64(pos64, wl.lambda_m, ordered=wl.ordered)
+    pairs = [(a, b) for a in range(wl.nsat) for b in range(wl.nsat) if (a != b if wl.ordered else a < b)]
+    packed = np.array([a | (b << 16) for a, b in pairs], np.int32)
+    snap = np.repeat(np.arange(pos64.shape[0], dtype=np.int32), len(pairs))
+    pair = np.tile(packed, pos64.shape[0])
+    l, m, n, b = S.make_sky(wl)
+    return wl, dict(u=u, v=v, w=w, snap=snap, pair=pair, sat_pos=pos64.astype(np.float32), l=l, m=m, n=n, b=b)
+
+
 def run_reference(args, ws, rank, local):
+    """The reference's CPU implementation of the path (the FP64 restatement of
+    visscal / imagerecon, oracle/viss_oracle.cpp, every host thread) on a bounded
+    sample of the same workload per step: nr visibilities x all J pixels (vis) and
+    np_ pixels x all K visibilities (recon), both multiples of the thread count so
+    that every thread gets the same share.  Where the reference's own kernels were
+    built from its sources (oracle/_ref), their full-size GPU timings are added as
+    ref_cuda_* keys.  Nothing here loads the product library."""
     if rank != 0:
         return
     import numpy as np
-    import torch
     from oracle import oracle as O
     O.build()
-    wl, d = load_workload(args.workload)
-    h = lambda t: t.cpu().numpy()  # noqa: E731
-    u, v, w, snap, pair, pos = (h(d[k]) for k in ("u", "v", "w", "snap", "pair", "sat_pos"))
-    l, m, n, b = (h(d[k]) for k in ("l", "m", "n", "b"))
+    wl, d = reference_workload(args.workload)
+    u, v, w, snap, pair, pos = (d[k] for k in ("u", "v", "w", "snap", "pair", "sat_pos"))
+    l, m, n, b = (d[k] for k in ("l", "m", "n", "b"))
     K, J = u.size, l.size
     thr = O.max_threads()
     ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=1.0, n_offset=-1.0, occluded_value=0.0, norm=1.0 / K)
     geo_all = O.make_geo(pos, snap, pair)
-    # bounded sample per step: nr rows x J (vis) + np_ pixels x K (recon), ~3 s
-    rows = np.arange(0, K, max(1, K // 32))[:32]
+    # calibrate on 4 rows a thread, then size the sample to ~cpu_seconds / 4 per step
+    rows = np.linspace(0, K - 1, 4 * thr).astype(np.int64)
     t0 = time.perf_counter()
     O.vis_dft(ocfg, u[rows], v[rows], w[rows], l, m, n, b, geo=O.make_geo(pos, snap[rows], pair[rows]), nthreads=thr)
     rate = rows.size * J / (time.perf_counter() - t0)
-    tgt = rate * 3.0
-    nr = int(min(K, max(32, tgt / 2 / J)))
-    np_ = int(min(J, max(8, tgt / 2 / K)))
+    tgt = rate * args.cpu_seconds / 4.0
+    whole = lambda x, cap: int(min(cap, max(thr, round(x / thr) * thr)))  # noqa: E731
+    nr = whole(tgt / 2 / J, K)
+    np_ = whole(tgt / 2 / K, J)
     ridx = np.linspace(0, K - 1, nr).astype(np.int64)
     pidx = np.linspace(0, J - 1, np_).astype(np.int64)
     geo_r = O.make_geo(pos, snap[ridx], pair[ridx])
@@ -460,10 +509,12 @@ def run_reference(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded orbit + Fibonacci sky)",
             "impl": "reference",
-            "config": {"workload": wl.name, "K": K, "J": J, "mask": "geometric"},
+            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws),
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": thr, "kind": "port",
-                             "sample": f"per step {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities, "
-                                       "FP64 restatement of visscal/imagerecon (oracle/viss_oracle.cpp)"},
+                             "sample": f"per step {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities "
+                                       f"({nr * J + np_ * K:.3g} terms), FP64 restatement of visscal/imagerecon "
+                                       "(oracle/viss_oracle.cpp) with the geometric mask, OpenMP on every host "
+                                       "thread"},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if not args.no_ref_cuda:
         line["ref_cuda_plain"] = ref_cuda_plain(wl, d)
@@ -473,28 +524,38 @@ def run_reference(args, ws, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def reference_windows(u, v, w, RES):
+    """Normalised REF windows [K, 4] (CUDA int32) from the reference's own stage 2:
+    its Cart2SphKernel and ShadeMatrix (oracle/ref_cuda.py), its thrust mean radius
+    restated (oracle/ref_thrust.cu), then the normalisation on load
+    (vissGen10M_shade.cu:383-399)."""
+    import torch
+    from oracle import ref_cuda, ref_thrust
+    _, mean_r = ref_thrust.mean_r(ref_cuda.cart2sph_r(u, v, w))
+    raw = ref_cuda.shade_windows(u, v, w, RES, mean_r)
+    t, p = raw[:, :2], raw[:, 2:]
+    return torch.stack([t.min(1).values - 1, t.max(1).values - 1, p.min(1).values - 1, p.max(1).values - 1], 1)
+
+
 def ref_cuda_plain(wl, d, variant="vissGen10M_shade"):
     """The reference's own kernels (visscal + imagerecon of `variant`: vissGen10M_shade,
     or its _optim1 / _optim2 rewrites; compiled from its sources into oracle/_ref) on
-    the full workload, with its REF window mask from the product's shade windows
-    (RES 20940)."""
+    the full workload, with its REF window mask (RES 20940) from its own stage 2."""
     try:
         import torch
         from oracle import ref_cuda
-        import viss_recon_shade_gb300 as V
         if not ref_cuda.available():
             return {"unavailable": "reference kernels not built (oracle/_ref missing)"}
-        K, J = d["u"].numel(), d["l"].numel()
+        t = {k: torch.from_numpy(d[k]).cuda() for k in ("u", "v", "w", "l", "m", "n", "b")}
+        K, J = t["u"].numel(), t["l"].numel()
         RES = 20940
-        raw, _ = V.shade_windows(d["u"], d["v"], d["w"], RES)
-        M = V.normalise_shade(raw)
-        Ms = [M[:, i].contiguous() for i in range(4)]
-        FF = d["b"]
+        Ms = [x.contiguous() for x in reference_windows(t["u"], t["v"], t["w"], RES).unbind(1)]
+        FF = t["b"]
         nxq = torch.arange(J, dtype=torch.float32, device="cuda")
         cl = torch.ones(J, dtype=torch.int32, device="cuda")
         wgt = torch.ones(K, dtype=torch.float32, device="cuda")
-        nclip = d["n"].clamp(-1, 1)
-        args = (d["u"], d["v"], d["w"], d["l"], d["m"], nclip)
+        nclip = t["n"].clamp(-1, 1)
+        args = (t["u"], t["v"], t["w"], t["l"], t["m"], nclip)
         st = torch.cuda.current_stream()
         # warm both kernels on a slice (module load, first launch)
         v0 = ref_cuda.visscal(variant, 8192, J, RES, FF, *args, *[x[:8192] for x in Ms], nxq, cl)
@@ -512,7 +573,7 @@ def ref_cuda_plain(wl, d, variant="vissGen10M_shade"):
         return {"value": round(2.0 * K * J / (ms * 1e-3) / 1e9, 3), "unit": UNIT,
                 "vis_ms": round(e0.elapsed_time(e1), 1), "recon_ms": round(e1.elapsed_time(e2), 1),
                 "what": f"reference {variant} visscal + imagerecon, unmodified device code, "
-                        "REF window mask, one pass"}
+                        "REF window mask from the reference's own shade windows, one pass"}
     except Exception as e:  # reported, not fatal: the CPU line above is the reference arm
         return {"unavailable": f"{type(e).__name__}: {e}"}
 

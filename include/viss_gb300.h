@@ -140,9 +140,14 @@ VISS_API int viss_vis_dft(const viss_dft_cfg* cfg, const viss_sky* sky, const vi
  * partial sums are the largest part of the scratch); passes that still need more
  * than the scratch are rejected with VISS_ERR_RANGE (131,072 visibilities x
  * 196,608 pixels with the geometric mask fit; the full 1,835,008 x 196,608
- * workload does not).  The first call on a device looks up the array's
- * device address; make it before any stream capture.  Calls share the array:
- * calls that overlap on the GPU race. */
+ * workload does not).  Every call looks up the array's device address on the
+ * current device (so a device reset does not leave a stale address); the first
+ * call on a device, or after a reset, loads the library's device code: make it
+ * before any stream capture.  The caller cannot reach the scratch to read the
+ * pass's input checks (viss_workspace_flags), so the call waits for the pass
+ * (synchronises `stream`) and returns them: VISS_ERR_RANGE for |uvw| >= 2^30,
+ * VISS_ERR_INVALID for a snapshot or satellite index outside the geometry.
+ * Calls share the array: calls that overlap on the GPU race. */
 #define VISS_NOALLOC_SCRATCH_BYTES (32u << 20)
 VISS_API int viss_vis_dft_noalloc(const viss_dft_cfg* cfg, const viss_sky* sky, const viss_vis_set* vis,
                                   const viss_geometry* geo, float* V, void* stream);

@@ -45,7 +45,7 @@ def _check(rc, what):
 
 
 def available() -> bool:
-    return (REF_DIR / "vissGen10M_shade.cubin").exists() or (REF_DIR / "vissGen10M_shade.ptx").exists()
+    return (REF_DIR / "vissGen10M_shade.cubin").exists()
 
 
 class RefModule:
@@ -59,15 +59,7 @@ class RefModule:
         _check(d.cuInit(0), "cuInit")
         self.mod = C.c_void_p()
         cubin = REF_DIR / f"{name}.cubin"
-        ptx = REF_DIR / f"{name}.ptx"
-        rc = -1
-        if cubin.exists():
-            rc = d.cuModuleLoad(C.byref(self.mod), str(cubin).encode())
-        if rc != 0 and ptx.exists():
-            data = ptx.read_bytes() + b"\0"
-            self._ptx = C.create_string_buffer(data)
-            rc = d.cuModuleLoadData(C.byref(self.mod), self._ptx)
-        _check(rc, f"cuModuleLoad({name})")
+        _check(d.cuModuleLoad(C.byref(self.mod), str(cubin).encode()), f"cuModuleLoad({name})")
         cnt = C.c_uint()
         _check(d.cuModuleGetFunctionCount(C.byref(cnt), self.mod), "cuModuleGetFunctionCount")
         funcs = (C.c_void_p * cnt.value)()
@@ -249,6 +241,36 @@ def orbit_uvw(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14
     return (xt[:S * nsat].view(nsat, S), yt[:S * nsat].view(nsat, S), zt[:S * nsat].view(nsat, S)), torch.stack(uvws)
 
 
+def host_r0(mean_r: float) -> float:
+    """r0 = atanf(1737.74f / (mean_r + 1737.74f)) with the host's float arithmetic and
+    libm's atanf, as the reference's host code computes it (shade1M.cu:222).  The
+    float sum and quotient are evaluated in double and rounded once, which gives the
+    correctly rounded float results that the host's float operations give."""
+    f = lambda x: C.c_float(x).value  # noqa: E731
+    libm = C.CDLL("libm.so.6")
+    libm.atanf.restype = C.c_float
+    libm.atanf.argtypes = [C.c_float]
+    return float(libm.atanf(f(f(1737.74) / f(f(mean_r) + f(1737.74)))))
+
+
+def cart2sph_r(u, v, w):
+    """The r array of the reference's Cart2SphKernel (shade1M.cu:63-70): K complex<float>
+    (imaginary parts 0) as a K x 2 float32 tensor."""
+    import torch
+    mod = module("shade1M")
+    K = u.numel()
+    cu = torch.stack([u, torch.zeros_like(u)], -1).contiguous()
+    cv = torch.stack([v, torch.zeros_like(v)], -1).contiguous()
+    cw = torch.stack([w, torch.zeros_like(w)], -1).contiguous()
+    th = torch.zeros(K, 2, dtype=torch.float32, device="cuda")
+    ph = torch.zeros_like(th)
+    r = torch.zeros_like(th)
+    bs = mod.occupancy_block("Cart2SphKernel")
+    mod.launch("Cart2SphKernel", (K + bs - 1) // bs, bs, [ptr(cu), ptr(cv), ptr(cw), ptr(th), ptr(ph), ptr(r), i32(K)])
+    torch.cuda.synchronize()
+    return r
+
+
 def shade_windows(u, v, w, RES, mean_r):
     """Cart2SphKernel + ShadeMatrix (shade1M.cu:63-105) on complex<float> arrays
     with zero imaginary parts; mean_r is supplied by the caller."""
@@ -265,8 +287,7 @@ def shade_windows(u, v, w, RES, mean_r):
     bs = mod.occupancy_block("Cart2SphKernel")
     mod.launch("Cart2SphKernel", (K + bs - 1) // bs, bs, [ptr(cu), ptr(cv), ptr(cw), ptr(th), ptr(ph), ptr(r), i32(K)])
     mean_rf = C.c_float(mean_r).value
-    r0 = math.atan(C.c_float(1737.74).value / C.c_float(mean_rf + C.c_float(1737.74).value).value)
-    r0 = C.c_float(r0).value
+    r0 = host_r0(mean_rf)
     dtheta = C.c_float(2 * math.pi / RES).value
     dphi = C.c_float(math.pi / RES).value
     sh = torch.zeros(K * 4, 2, dtype=torch.float32, device="cuda")

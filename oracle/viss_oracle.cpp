@@ -197,7 +197,7 @@ ORACLE_API int oracle_vis_dft(const oracle_dft_cfg* cfg, const float* u, const f
                               const float* m, const float* n, const float* bright, int64_t J,
                               double* V, int nthreads) {
   const double s = cfg->phase_scale, noff = cfg->n_offset;
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t k = 0; k < K; ++k) {
     const double uk = u[k], vk = v[k], wk = w[k];
     double re = 0.0, im = 0.0;
@@ -228,7 +228,7 @@ ORACLE_API int oracle_vis_dft_windex(const oracle_dft_cfg* cfg, const float* u, 
                                      const float* m, const float* n, const float* bright, int64_t J, double* V,
                                      int nthreads) {
   const double s = cfg->phase_scale, noff = cfg->n_offset;
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t k = 0; k < K; ++k) {
     const double uk = u[k], vk = v[k], wk = w[k];
     double re = 0.0, im = 0.0;
@@ -260,7 +260,7 @@ ORACLE_API int oracle_vis_dft_nxq(const oracle_dft_cfg* cfg, const float* u, con
   const double s = cfg->phase_scale, noff = cfg->n_offset;
   std::vector<int64_t> start(J + 1, 0);
   for (int64_t j = 0; j < J; ++j) start[j + 1] = start[j] + countLoc[j];
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t k = 0; k < K; ++k) {
     const int32_t* M = shade ? shade + 4 * k : nullptr;
     double re = 0.0, im = 0.0;
@@ -309,7 +309,7 @@ ORACLE_API int oracle_recon(const oracle_dft_cfg* cfg, const float* u, const flo
       r2[k] = (float)shade[4 * k + 2] / (float)shade[4 * k + 3];
     }
   }
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t j = 0; j < J; ++j) {
     const float phiP = std::floor((float)(j / cfg->res));
     const float thetaP = (float)j - phiP * (float)cfg->res;
@@ -348,7 +348,7 @@ ORACLE_API int oracle_vis_plain_f32(const oracle_dft_cfg* cfg, const float* u, c
                                     const float* m, const float* n, const float* FF, int64_t J,
                                     float d, float* V, int nthreads, int optim) {
   const float two_pi_f = -2.0f * (float)kPi;  // (0 - i) * 2 * pi, imaginary part
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t k = 0; k < K; ++k) {
     float ar = 0.f, ai = 0.f;
     for (int64_t j = 0; j < J; ++j) {
@@ -385,7 +385,7 @@ ORACLE_API int oracle_recon_plain_f32(const oracle_dft_cfg* cfg, const float* u,
       r2[k] = (float)shade[4 * k + 2] / (float)shade[4 * k + 3];
     }
   }
-#pragma omp parallel for schedule(dynamic, 16) num_threads(nthreads_or_default(nthreads))
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads_or_default(nthreads))
   for (int64_t j = 0; j < J; ++j) {
     const float phiP = std::floor((float)(j / cfg->res));
     const float thetaP = (float)j - phiP * (float)cfg->res;

@@ -449,8 +449,7 @@ def recon_ratios(shade: torch.Tensor):
 
 
 # ---------------------------------------------------------------- orbit + uvw
-REF_R1 = (0.0, 1e3, 4.45e3, 6e3, 9.1e3, 16.2e3, 35.3e3, 100e3)      # MIncline_generate_uvw_float.cu:29
-REF_R2 = (0.0, 0.1e3, 0.445e3, 0.6e3, 0.91e3, 1.62e3, 3.53e3, 10e3)  # :30
+from .synth import REF_R1, REF_R2  # noqa: E402  (MIncline_generate_uvw_float.cu:29-30)
 
 
 @dataclass(frozen=True)

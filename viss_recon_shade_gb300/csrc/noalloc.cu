@@ -11,41 +11,27 @@
 //
 // The scratch is a file-scope __device__ array of VISS_NOALLOC_SCRATCH_BYTES
 // (32 MiB).  Every GPU that loads the library keeps it resident until the
-// process exits.  Host code cannot use the array's name as a device address;
-// the first call on each device asks the runtime for that device's address
-// (cudaGetSymbolAddress, with the device current) and caches it, so that first
-// call on a device should come before any stream capture.  All calls share the
-// one buffer and it keeps the previous call's contents: the pass clears what
-// must start at zero (its flag words) itself, and calls whose work overlaps on
-// the GPU (different streams or threads without ordering) race on the buffer.
-#include <mutex>
-
+// process exits.  Host code cannot use the array's name as a device address:
+// every call asks the runtime for the current device's address of the array
+// (cudaGetSymbolAddress, with that device current).  After the module is
+// loaded this is a host-side lookup, and because it is repeated on every call a
+// context torn down and rebuilt (cudaDeviceReset) gets the new address.  The
+// first call on a device (or after a reset) loads the module, so it should come
+// before any stream capture.  All calls share the one buffer and it keeps the
+// previous call's contents: the pass clears what must start at zero (its flag
+// words) itself, and calls whose work overlaps on the GPU (different streams or
+// threads without ordering) race on the buffer.
+//
+// The pass records input problems in the scratch's flag words instead of
+// reading out of bounds (viss_workspace_flags reads them for a caller
+// workspace).  A caller of this entry point cannot reach the scratch, so the
+// call reads them itself once the pass has completed: it synchronises `stream`
+// and returns the problem as a status.
 #include "viss_internal.cuh"
 
 namespace viss {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[VISS_NOALLOC_SCRATCH_BYTES];
-
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on the current device (set up once per device).
-int scratch_address(void** out) {
-  int dev = 0;
-  VISS_CUDA(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(VISS_ERR_UNSUPPORTED, "device ordinal beyond the scratch table");
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    VISS_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_addr[dev] = p;
-  }
-  *out = g_scratch_addr[dev];
-  return VISS_OK;
-}
-}  // namespace
 
 }  // namespace viss
 
@@ -70,9 +56,22 @@ extern "C" int viss_vis_dft_noalloc(const viss_dft_cfg* cfg, const viss_sky* sky
                                     " bytes of scratch, more than the built-in " +
                                     std::to_string((size_t)VISS_NOALLOC_SCRATCH_BYTES) +
                                     " (use viss_vis_dft with a caller workspace)");
+  // the current device's address of the array, looked up on every call
   void* scratch = nullptr;
-  int rc = scratch_address(&scratch);
-  if (rc) return rc;
+  VISS_CUDA(cudaGetSymbolAddress(&scratch, g_noalloc_scratch));
   // the same checks and pass as viss_vis_dft, on the built-in scratch
-  return viss_vis_dft_batch(cfg, sky, vis, nullptr, geo, &tn, V, scratch, (size_t)VISS_NOALLOC_SCRATCH_BYTES, stream);
+  int rc = viss_vis_dft_batch(cfg, sky, vis, nullptr, geo, &tn, V, scratch, (size_t)VISS_NOALLOC_SCRATCH_BYTES,
+                              stream);
+  if (rc != VISS_OK || vis->K == 0 || sky->J == 0) return rc;
+  // input problems the pass recorded (the flag words are the scratch's first carve)
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int32_t err = 0;
+  VISS_CUDA(cudaMemcpyAsync(&err, static_cast<const int32_t*>(scratch) + FLAG_ERR, sizeof(err),
+                            cudaMemcpyDeviceToHost, st));
+  VISS_CUDA(cudaStreamSynchronize(st));
+  if (err & 1) return fail(VISS_ERR_RANGE, "viss_vis_dft_noalloc: a |u|, |v| or |w| of 2^30 or more");
+  if (err & 2)
+    return fail(VISS_ERR_INVALID, "viss_vis_dft_noalloc: a snapshot or satellite index outside the geometry");
+  if (err) return fail(VISS_ERR_INVALID, "viss_vis_dft_noalloc: input flags " + std::to_string(err));
+  return VISS_OK;
 }

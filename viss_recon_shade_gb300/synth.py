@@ -4,6 +4,9 @@ The reference reads MATLAB-generated sky and uvw files that are not part of
 it; these generators stand in for them: Fibonacci-sphere pixels, log-normal or
 power-law diffuse skies with point sources deposited on the nearest pixel,
 and lunar orbits driven through the product's own orbit/uvw kernels.
+
+Everything above make_orbit_cfg needs numpy only (the module also loads on its
+own, by path, without the product library).
 """
 from __future__ import annotations
 
@@ -12,6 +15,9 @@ from dataclasses import dataclass
 import numpy as np
 
 MOON_R = 1737.4
+# along-track separation ramps of the reference's 8 satellites, r1 -> r2 -> r1 (m)
+REF_R1 = (0.0, 1e3, 4.45e3, 6e3, 9.1e3, 16.2e3, 35.3e3, 100e3)      # MIncline_generate_uvw_float.cu:29
+REF_R2 = (0.0, 0.1e3, 0.445e3, 0.6e3, 0.91e3, 1.62e3, 3.53e3, 10e3)  # :30
 
 
 def fibonacci_sphere(J: int):
@@ -46,7 +52,6 @@ def log_separations(nsat: int, dmax_m: float = 100e3):
     """Along-track separation ramps for nsat satellites, 0 .. dmax (r1) and dmax/10 (r2),
     log-spaced like the reference's 8 (MIncline_generate_uvw_float.cu:29-30)."""
     if nsat == 8:
-        from .api import REF_R1, REF_R2
         return tuple(REF_R1), tuple(REF_R2)
     r1 = np.concatenate([[0.0], np.geomspace(1e3, dmax_m, nsat - 1)])
     return tuple(float(x) for x in r1), tuple(float(x) / 10.0 for x in r1)
