@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--no-stage1", action="store_true", help="skip the stage-1 (uvw generation) record")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-channel record")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -364,15 +365,86 @@ def run_ours(args, ws, rank, local):
         # the record; `--workload stage1` reports it in full
         del Vout, Fout, flush
         torch.cuda.empty_cache()
-        K1, n1, ms1, _ = stage1_passes(3, 3)
+        K1, n1, ms1, (_, uu, vv, ww) = stage1_passes(3, 3)
         line["stage1"] = {"value": round(K1 / (sum(ms1) * 1e-3) / 1e9, 3), "unit": "G uvw rows/s",
                           "ms_per_pass": round(sum(ms1), 2), "uvw_rows": K1, "unique_rows": n1,
                           "stage_ms": {"positions": round(ms1[0], 2), "unique_fused": round(ms1[1], 2)},
                           "what": "MIncline_generate_uvw_float at its own size (8 satellites, 864,000 samples "
                                   "an orbit, 140 orbits, 10 MHz): positions + viss_unique_uvw"}
+        if not args.no_ref_cuda:
+            line["stage1"]["reference"], line["stage2"] = reference_stages(uu, vv, ww, K1)
+        del uu, vv, ww
+        torch.cuda.empty_cache()
+    if not args.no_batch and ws == 1:
+        # the batched multi-channel configuration (64 channels, one persistent graph-replayed
+        # launch per pass); `--workload batch64` reports it as its own line
+        if "Vout" in locals():
+            del Vout, Fout, flush
+            torch.cuda.empty_cache()
+        b = batch_record("batch64", 3, 2, args.precision, sfu_peak=sfu_peak)
+        line["batch64"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "vis_ms", "recon_ms", "roofline",
+                                             "plain_per_channel", "speedup_vs_plain", "accuracy", "clocks",
+                                             "gpu_launches_per_step")}
+        line["batch64"]["config"] = {k: b["config"][k] for k in ("workload", "channels", "K", "J", "terms_per_step",
+                                                                  "launch")}
+        line["batch64"]["autotune_best"] = b["autotune"]["best"]
         torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def reference_stages(uu, vv, ww, K1, RES=20940):
+    """The reference's own stage 1 and stage 2 on the same GPU, beside ours.
+    Stage 1 (MIncline_generate_uvw_float.cu:215-397 at its size): its orbit, window and
+    computeUVW kernels from its sources, per ordered pair thrust::sort + unique with its
+    comparators (restated, oracle/ref_thrust.cu), the concatenation and the global
+    sort + unique -- compared row for row (bitwise) with ours (uu, vv, ww).  Stage 2
+    (shade10M.cu:188-224, RES 20940) on those unique rows: its Cart2SphKernel, its FP32
+    thrust mean radius (restated; it copies r into a device_vector first, as the
+    reference's r is one) and ShadeMatrix, against viss_shade_windows on the same rows."""
+    import torch
+    try:
+        import viss_recon_shade_gb300 as V
+        from oracle import ref_cuda, ref_thrust
+        from viss_recon_shade_gb300.synth import REF_R1, REF_R2
+        if not ref_cuda.available():
+            return {"unavailable": "reference kernels not built (oracle/_ref missing)"}, None
+        cfg = V.OrbitConfig()
+        ref_cuda.mincline_unique(8, 8640, 2, 1, 1e7, REF_R1, REF_R2)  # module loads, first launches
+        rows, ms = ref_cuda.mincline_unique(cfg.nsat, cfg.orbit_res, cfg.orbit_counts, 1, 1e7, REF_R1, REF_R2,
+                                            timed=True)
+        ours = torch.stack([uu, vv, ww], 1)
+        same1 = rows.shape == ours.shape and torch.equal(rows.view(torch.int32), ours.view(torch.int32))
+        s1 = {"value": round(K1 / (ms["total"] * 1e-3) / 1e9, 3), "unit": "G uvw rows/s",
+              "ms_per_pass": round(ms["total"], 1),
+              "stage_ms": {k: round(v, 1) for k, v in ms.items() if k != "total"}, "unique_rows": int(rows.shape[0]),
+              "identical_rows": bool(same1),
+              "what": "the reference's calculateOrbit / uvwPosition / computeUVW kernels (its sources) + per-pair "
+                      "thrust sort/unique with its comparators + global sort/unique (thrust, restated)"}
+        del rows
+        u, v, w = (x.contiguous() for x in (uu, vv, ww))
+        st = torch.cuda.current_stream()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ref_cuda.shade_windows(u[:4096], v[:4096], w[:4096], RES, 3000.0)  # warm
+        V.shade_windows(u, v, w, RES)
+        torch.cuda.synchronize()
+        ev[0].record(st)
+        _, mean_r = ref_thrust.mean_r(ref_cuda.cart2sph_r(u, v, w))
+        ref_win, _ = ref_cuda.shade_windows(u, v, w, RES, mean_r)
+        ev[1].record(st)
+        win, m_ours = V.shade_windows(u, v, w, RES)
+        ev[2].record(st)
+        torch.cuda.synchronize()
+        ref_ms, our_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+        n = u.numel()
+        s2 = {"value": round(n / (our_ms * 1e-3) / 1e9, 2), "unit": "G rows/s", "rows": n, "res": RES,
+              "ms": round(our_ms, 3),
+              "reference": {"value": round(n / (ref_ms * 1e-3) / 1e9, 2), "unit": "G rows/s", "ms": round(ref_ms, 3)},
+              "identical_windows": bool(torch.equal(ref_win, win)), "mean_r_equal": bool(float(m_ours) == mean_r),
+              "what": "shade windows of the stage-1 rows: Cart2Sph + FP32 mean radius + ShadeMatrix"}
+        return s1, s2
+    except Exception as e:  # reported, not fatal
+        return {"unavailable": f"{type(e).__name__}: {e}"}, None
 
 
 def cpu_baseline(args, wl, d, Vout, Fout, cfg):
@@ -532,7 +604,7 @@ def reference_windows(u, v, w, RES):
     import torch
     from oracle import ref_cuda, ref_thrust
     _, mean_r = ref_thrust.mean_r(ref_cuda.cart2sph_r(u, v, w))
-    raw = ref_cuda.shade_windows(u, v, w, RES, mean_r)
+    raw, _ = ref_cuda.shade_windows(u, v, w, RES, mean_r)
     t, p = raw[:, :2], raw[:, 2:]
     return torch.stack([t.min(1).values - 1, t.max(1).values - 1, p.min(1).values - 1, p.max(1).values - 1], 1)
 
@@ -580,22 +652,30 @@ def ref_cuda_plain(wl, d, variant="vissGen10M_shade"):
 
 # ------------------------------------------------------------------ batched channels
 def run_batch(args, ws, rank, local):
-    """--workload batch64: 64 channels log-spaced over 1-30 MHz, 28 baselines x
-    U[4096, 65536] snapshots each, 49,152 pixels with per-channel power-law
-    brightness, geometric mask; one persistent vis launch + one persistent recon
-    launch per step, replayed from a CUDA graph, launch parameters from the
-    autotuner (timed on every 8th channel).  Compared with the reference's form:
-    per-channel plain launches, timed on 4 channels spread over the band."""
+    """--workload batch64: the batched-channel line (batch_record)."""
+    line = batch_record(args.workload, args.steps, args.warmup, args.precision, ws, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def batch_record(workload, steps, warmup, precision, ws=1, local=0, sfu_peak=None):
+    """64 channels log-spaced over 1-30 MHz, 28 baselines x U[4096, 65536] snapshots
+    each, 49,152 pixels with per-channel power-law brightness, geometric mask; one
+    persistent vis launch + one persistent recon launch per step, replayed from a
+    CUDA graph, launch parameters from the autotuner (timed on every 8th channel).
+    Compared with the reference's form: per-channel plain launches, timed on 4
+    channels spread over the band.  With sfu_peak (G SFU op/s) the dominant pass's
+    roofline fraction is added."""
     import numpy as np
     import torch
     import viss_recon_shade_gb300 as V
     from viss_recon_shade_gb300 import _lib as L
     from viss_recon_shade_gb300.synth import BATCH_WORKLOADS, make_batch
-    bw = BATCH_WORKLOADS[args.workload]
+    bw = BATCH_WORKLOADS[workload]
     d = make_batch(bw)
     t = lambda a: torch.from_numpy(a).cuda()  # noqa: E731
     lg, mg, ng = t(d["l"]), t(d["m"]), t(d["n"])
-    prec = choose_precision(d, args.precision)
+    prec = choose_precision(d, precision)
     cfg = V.DftConfig.geometric(precision=prec, occluded_value=0.0)
     ro = d["row_off"]
     K, J, nch = int(ro[-1]), bw.J, bw.nch
@@ -620,7 +700,7 @@ def run_batch(args, ws, rank, local):
     b.set_tuning(best)
     g = b.graph()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         flush.zero_()  # as in a timed step (see run_ours)
         g.replay()
     torch.cuda.synchronize()
@@ -630,7 +710,7 @@ def run_batch(args, ws, rank, local):
         barrier(ws)
         torch.cuda.synchronize()
         t0e.record(st)
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             g.replay()
         t1e.record(st)
@@ -638,7 +718,7 @@ def run_batch(args, ws, rank, local):
         barrier(ws)
     total_ms = max_over_ranks(t0e.elapsed_time(t1e), ws)
     terms_step = 2.0 * K * J
-    value = terms_step * args.steps * ws / (total_ms * 1e-3) / 1e9
+    value = terms_step * steps * ws / (total_ms * 1e-3) / 1e9
     # split of one eager step
     e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
     n0 = L.lib.viss_launch_count()
@@ -667,7 +747,7 @@ def run_batch(args, ws, rank, local):
     plain_value = pterms / (p0.elapsed_time(p1) * 1e-3) / 1e9
     names = {V.PREC_FAST: "fast", V.PREC_COMPENSATED: "compensated"}
     line = {"metric": "Gterms/s batched shaded vis-DFT + recon, 1 GB300", "value": round(value, 3), "unit": UNIT,
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3),
+            "n_gpus": ws, "steps": steps, "warmup": warmup, "ms_per_step": round(total_ms / steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fixed-point i32 phase)",
             "data": "synthetic (seeded orbits per channel + Fibonacci sky)",
             "config": {"workload": bw.name, "channels": nch, "K": K, "J": J, "terms_per_step": int(terms_step),
@@ -680,8 +760,14 @@ def run_batch(args, ws, rank, local):
                                   "what": "PREC_PLAIN, one vis + one recon launch per channel"},
             "speedup_vs_plain": round(value / plain_value, 2), "accuracy": acc, "clocks": clk.summary(),
             "gpu_launches_per_step": launches}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
+    if sfu_peak:
+        dom_ms, dom = (vis_ms, "vis_fast_kernel") if vis_ms >= rec_ms else (rec_ms, "recon_fast_kernel")
+        achieved = 2.0 * K * J / (dom_ms * 1e-3) / 1e9
+        line["roofline"] = {"bound": "sfu", "kernel": dom, "achieved": round(achieved, 2), "peak": round(sfu_peak, 2),
+                            "unit": "G SFU op/s", "frac": round(achieved / sfu_peak, 4),
+                            "peak_source": "measured: viss_sfu_probe in this run",
+                            "achieved_from": "2 SFU ops x K x J / the pass's CUDA-event time (one eager step)"}
+    return line
 
 
 def batch_accuracy(d, b, cfg):

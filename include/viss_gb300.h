@@ -75,7 +75,10 @@ enum {                         /* recon-side mask */
 enum {                         /* phase + sincos arithmetic */
   VISS_PREC_PLAIN = 0,         /* the reference's FP32 formula, precise sinf/cosf, 1 thread per item */
   VISS_PREC_FAST = 1,          /* 32-bit fixed-point phase (exact mod 1 for integer uvw), SFU sincos */
-  VISS_PREC_COMPENSATED = 2    /* FAST + FP32 correction of the pixel fixed-point rounding */
+  VISS_PREC_COMPENSATED = 2,   /* FAST + FP32 correction of the pixel fixed-point rounding */
+  VISS_PREC_F64_PHASE = 3      /* precision sweeps (no counterpart in the reference): the phase in FP64,
+                                  range-reduced in FP64, FP32 sincosf, Kahan-compensated FP32 sums;
+                                  one thread per item like PLAIN, and slow (GB300's FP64 rate) */
 };
 
 /* One DFT pass.  Phase in turns: t = phase_scale * (u l + v m + w (n + n_offset)).

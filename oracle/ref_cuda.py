@@ -173,20 +173,48 @@ def imagerecon(variant: str, K, J, res, viss, u, v, w, l, m, n, wgt, M1, M2, M3,
     return F
 
 
-def orbit_uvw(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14, e=0.0,
-              incl_deg=30.0, argp_deg=0.0, mu=4.902793455e3):
-    """calculateOrbit + uvwPosition per satellite, then computeUVW per ordered
-    pair (MIncline_generate_uvw_float.cu:215-368).  Returns xt,yt,zt [nsat][S]
-    and uvw [pairs][S][3] (before the thrust sort/unique).
+def mincline_unique(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14, e=0.0, incl_deg=30.0,
+                    argp_deg=0.0, mu=4.902793455e3, timed=False):
+    """The reference's whole uvw stage (MIncline_generate_uvw_float.cu:215-397): its
+    calculateOrbit / uvwPosition kernels per satellite, then per ordered pair its
+    computeUVW kernel followed by thrust::sort + thrust::unique (restated in
+    oracle/ref_thrust.cu) and the append to a global list, which is sorted and
+    uniqued at the end.  Returns the unique rows [n, 3] (float32, CUDA) and, with
+    timed=True, a dict of CUDA-event milliseconds {positions, pairs, global, total}."""
+    import torch
+    from oracle import ref_thrust
+    ref_thrust.lib()  # load (and build) before the timed region
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    st = torch.cuda.current_stream()
+    ev[0].record(st)
+    mod, (xt, yt, zt), S, nblk, bs3, lam = _positions(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a, e,
+                                                      incl_deg, argp_deg, mu)
+    ev[1].record(st)
+    hash_ = torch.zeros(nblk * bs3, 3, dtype=torch.float32, device="cuda")
+    parts = []
+    for mm in range(nsat):
+        for nn in range(nsat):
+            if mm == nn:
+                continue
+            mod.launch("computeUVW", nblk, bs3, [ptr(xt), ptr(yt), ptr(zt), ptr(hash_), i32(orbit_counts),
+                                                 i32(orbit_res), f32(lam), i32(mm), i32(nn)])
+            rows = hash_[:S]
+            parts.append(rows[:ref_thrust.sort_unique(rows)].clone())
+    glob = torch.cat(parts)
+    del parts
+    ev[2].record(st)
+    glob = glob[:ref_thrust.sort_unique(glob)]
+    ev[3].record(st)
+    torch.cuda.synchronize()
+    if not timed:
+        return glob
+    ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(3)]
+    return glob, {"positions": ms[0], "pairs": ms[1], "global": ms[2], "total": sum(ms)}
 
-    Host-side arrays are built as the reference's thrust code builds them
-    (linspace `a + step*x` contracted to one FMA, x the float sequence value;
-    dM in double, :42-58).  Two reference reads run past their buffers:
-    uvwPosition reads x[sat*total + total] when a window ends exactly at the
-    end (for the last satellite one element past the array), and computeUVW
-    has no bounds check on its rounded-up grid.  The buffers here are padded
-    (one extra satellite of zeros; one extra block of xt and of the output) so
-    both stay inside their allocations; the padding reads as zero."""
+
+def _positions(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a, e, incl_deg, argp_deg, mu):
+    """calculateOrbit + uvwPosition per satellite (MIncline_generate_uvw_float.cu:215-330):
+    windowed positions xt, yt, zt [nsat * S (+ a block of padding)]."""
     import math
     import numpy as np
     import torch
@@ -197,6 +225,7 @@ def orbit_uvw(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14
     lam = int(3e8 / frequency)
     fl = lambda x: float(np.float32(x))  # noqa: E731
     d2r = fl(math.pi / 180)
+    # one satellite of zeros beyond the last: uvwPosition reads one element past it
     x = torch.zeros(N * (nsat + 1), dtype=torch.float32, device="cuda")
     y = torch.zeros_like(x)
     z = torch.zeros_like(x)
@@ -225,9 +254,28 @@ def orbit_uvw(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14
         args = [ptr(x), ptr(y), ptr(z), ptr(xt), ptr(yt), ptr(zt), i32(orbit_counts), i32(orbit_res),
                 i32(interval), i32(span), i32(ss)]
         mod.launch("uvwPosition", (N // 3 + bs2 - 1) // bs2, bs2, args)
-        torch.cuda.synchronize()
-    uvws = []
     nblk = (S + bs3 - 1) // bs3
+    return mod, (xt, yt, zt), S, nblk, bs3, lam
+
+
+def orbit_uvw(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a=2038.14, e=0.0,
+              incl_deg=30.0, argp_deg=0.0, mu=4.902793455e3):
+    """calculateOrbit + uvwPosition per satellite, then computeUVW per ordered
+    pair (MIncline_generate_uvw_float.cu:215-368).  Returns xt,yt,zt [nsat][S]
+    and uvw [pairs][S][3] (before the thrust sort/unique).
+
+    Host-side arrays are built as the reference's thrust code builds them
+    (linspace `a + step*x` contracted to one FMA, x the float sequence value;
+    dM in double, :42-58).  Two reference reads run past their buffers:
+    uvwPosition reads x[sat*total + total] when a window ends exactly at the
+    end (for the last satellite one element past the array), and computeUVW
+    has no bounds check on its rounded-up grid.  The buffers here are padded
+    (one extra satellite of zeros; one extra block of xt and of the output) so
+    both stay inside their allocations; the padding reads as zero."""
+    import torch
+    mod, (xt, yt, zt), S, nblk, bs3, lam = _positions(nsat, orbit_res, orbit_counts, index, frequency, r1, r2, a, e,
+                                                      incl_deg, argp_deg, mu)
+    uvws = []
     hash_ = torch.zeros(nblk * bs3, 3, dtype=torch.float32, device="cuda")
     for mm in range(nsat):
         for nn in range(nsat):

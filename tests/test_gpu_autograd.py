@@ -1,8 +1,8 @@
 """Adjoint / autograd: the gradient of a visibility loss through the CUDA
 forward (viss_vis_dft) and adjoint (viss_recon) agrees with central finite
 differences on 64 random pixels and with the FP64 oracle gradient; a sky +
-per-baseline-gain fit reduces the loss (differentiable imaging at 10 MHz,
-28 baselines x 16,384 snapshots, 49,152 pixels, SNR 20)."""
+per-baseline-gain fit recovers the seeded sky and gains (differentiable imaging
+at 10 MHz, 28 baselines x 16,384 snapshots, 49,152 pixels, SNR 20)."""
 import numpy as np
 import pytest
 
@@ -68,19 +68,32 @@ def test_gradient_vs_finite_differences_and_fp64(setup, oracle):
     assert efd < 1e-4, efd
 
 
-def test_fit_sky_and_gains_reduces_loss(setup):
+def test_fit_recovers_sky_and_gains(setup):
+    """The cfg4 fit (100 Adam steps, non-negative sky + 28 complex baseline gains) recovers
+    the seeded truth.  The model g_b A(x) is invariant under x -> a x, g -> g / a, so the
+    gains are compared after the best complex scale c (c g closest to the true gains):
+    their error must be well below the spread of the true gains (i.e. the fit finds each
+    baseline's own gain, not just the mean), the sky must correlate with the truth, and
+    the misfit must sit at the noise level (SNR 20: |noise|^2 / |V|^2 ~ 1/400)."""
     V, wl, d, cfg = setup
     from viss_recon_shade_gb300.autograd import fit_sky_and_gains
     gen = torch.Generator(device="cuda").manual_seed(2)
     nb = wl.npairs
-    true_g = (1 + 0.05 * torch.randn(nb, generator=gen, device="cuda")) * torch.exp(
-        1j * 0.05 * torch.randn(nb, generator=gen, device="cuda"))
+    true_g = ((1 + 0.05 * torch.randn(nb, generator=gen, device="cuda")) * torch.exp(
+        1j * 0.05 * torch.randn(nb, generator=gen, device="cuda"))).to(torch.complex64)
     baseline = torch.arange(d["u"].numel(), device="cuda") % nb
-    Vt = forward(V, d, cfg, d["truth"]).detach() * true_g.to(torch.complex64)[baseline]
+    Vt = forward(V, d, cfg, d["truth"]).detach() * true_g[baseline]
     noise = (torch.randn(Vt.shape, generator=gen, device="cuda") + 1j * torch.randn(Vt.shape, generator=gen,
                                                                                         device="cuda")) / np.sqrt(2)
     V_obs = Vt + noise.to(torch.complex64) * Vt.abs().mean() / 20
     res = fit_sky_and_gains(V_obs, cfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["snap"], d["pair"],
                             d["sat_pos"], baseline, nb, steps=100)
-    assert res.losses[-1] < 0.2 * res.losses[0]
     assert torch.all(res.sky >= 0)
+    assert res.losses[-1] < 4.0 / 400 and res.losses[-1] < 0.01 * res.losses[0], res.losses[-1]
+    g = res.gains
+    c = (g.conj() * true_g).sum() / (g.abs() ** 2).sum()
+    err = ((c * g - true_g).abs() ** 2).mean().sqrt().item()
+    spread = ((true_g - true_g.mean()).abs() ** 2).mean().sqrt().item()
+    assert err < 0.3 * spread, (err, spread)
+    corr = torch.corrcoef(torch.stack([res.sky, d["truth"]]))[0, 1].item()
+    assert corr > 0.999, corr

@@ -94,6 +94,31 @@ def test_vissGen10M_shade_dropin(oracle, tmp_path):
     assert (tmp_path / "F_recon_10M" / "F1period10M_optim2.txt").exists()
 
 
+def test_vissGen10M_resume_skips_complete_periods(tmp_path):
+    """--resume: periods whose F_recon file already holds all J lines are skipped;
+    a truncated file (an interrupted run elsewhere) is recomputed, to the same bytes."""
+    J, K, res = 1024, 1024, 128
+    make_sky_dir(tmp_path / "lmn10M", J)
+    write_col(tmp_path / "lmn10M" / "countLoc.txt", np.ones(J))
+    write_col(tmp_path / "lmn10M" / "NXq.txt", np.arange(J))
+    fd = tmp_path / "frequency_10M"
+    fd.mkdir()
+    for p in (1, 2, 3):
+        u, v, w, raw = synth_uvw_shade(K, res, seed=10 + p)
+        np.savetxt(fd / f"updated_uvw{p}frequency10M.txt", np.stack([u, v, w, np.ones(K)], -1), fmt="%g")
+        np.savetxt(fd / f"shadeM{p}frequency10M.txt", raw, fmt="%d")
+    args = [BIN / "vissGen10M_shade", "--res", res, "--days", 3]
+    run(args, tmp_path)
+    outs = [tmp_path / "F_recon_10M" / f"F{p}period10M.txt" for p in (1, 2, 3)]
+    full = [o.read_bytes() for o in outs]
+    assert not list((tmp_path / "F_recon_10M").glob("*.part"))
+    outs[1].write_bytes(full[1][: len(full[1]) // 2])  # period 2 interrupted half way
+    outs[2].unlink()                                   # period 3 never written
+    log = run(args + ["--resume", 1], tmp_path)
+    assert "F1period10M.txt complete, skipped" in log and log.count("complete, skipped") == 1
+    assert [o.read_bytes() for o in outs] == full
+
+
 def test_vissGen1M_dropin_weights_and_expansion(oracle, tmp_path):
     J, K, res = 1024, 1024, 128
     fd = tmp_path / "frequency_1M"
@@ -140,7 +165,7 @@ def test_shade10M_dropin(tmp_path):
     ours = np.loadtxt(fd / "shadeM2frequency10M.txt", dtype=np.int64)
     tu, tv, tw = (torch.from_numpy(x).cuda() for x in (u, v, w))
     _, mean_r = RT.mean_r(refk.cart2sph_r(tu, tv, tw))
-    ref = refk.shade_windows(tu, tv, tw, 20940, mean_r).cpu().numpy()
+    ref = refk.shade_windows(tu, tv, tw, 20940, mean_r)[0].cpu().numpy()
     assert np.array_equal(ours, ref)
 
 
@@ -150,19 +175,12 @@ def test_mincline_dropin(tmp_path):
     default format, MIncline_generate_uvw_float.cu:421-427).  Reference rows: its
     calculateOrbit / uvwPosition / computeUVW kernels from its sources, then its
     per-pair sort + unique, concatenation and global sort + unique (thrust, restated)."""
-    import torch
-    refk, RT = _ref_kernels()
+    refk, _ = _ref_kernels()
     run([BIN / "MIncline_generate_uvw_float", "--periods", 1, "--orbit-res", 720, "--orbit-counts", 3], tmp_path)
     ours = (tmp_path / "frequency_10M" / "uvw1frequency10M.txt").read_text()
     r1 = [0, 1e3, 4.45e3, 6e3, 9.1e3, 16.2e3, 35.3e3, 100e3]
     r2 = [0, 0.1e3, 0.445e3, 0.6e3, 0.91e3, 1.62e3, 3.53e3, 10e3]
-    _, uvw = refk.orbit_uvw(8, 720, 3, 1, 1e7, r1, r2)  # [56 pairs][S][3], m-major ordered pairs
-    parts = []
-    for p in range(uvw.shape[0]):
-        rows = uvw[p].contiguous()
-        parts.append(rows[:RT.sort_unique(rows)].clone())
-    glob = torch.cat(parts).contiguous()
-    glob = glob[:RT.sort_unique(glob)].cpu().numpy()
+    glob = refk.mincline_unique(8, 720, 3, 1, 1e7, r1, r2).cpu().numpy()
     ref = "".join(f"{np.float32(a):g} {np.float32(b):g} {np.float32(c):g}\n" for a, b, c in glob.tolist())
     assert ours == ref
 

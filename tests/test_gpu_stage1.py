@@ -160,3 +160,21 @@ def test_unique_uvw_count_only_and_short_capacity(V):
     rc = L.lib.viss_unique_uvw(C.c_void_p(pos.data_ptr()), S, nsat, 1, 30.0, *ptrs, n, C.byref(cnt),
                                C.c_void_p(ws.data_ptr()), nb - 1, st)
     assert rc == L.VISS_ERR_WORKSPACE
+
+
+@pytest.mark.parametrize("orbit_res,orbit_counts,index", [(86400, 10, 1), (8640, 140, 3)])
+def test_unique_uvw_bitwise_vs_reference_pipeline(V, orbit_res, orbit_counts, index):
+    """The whole stage against the reference's own: its orbit, window and computeUVW
+    kernels (from its sources) + per-pair thrust sort/unique with its comparators and
+    the global sort/unique (restated) -- the same rows, bit for bit (signs of zero
+    included), as positions + viss_unique_uvw at 10 MHz, on millions of snapshots."""
+    from oracle import ref_cuda
+    if not ref_cuda.available():
+        pytest.skip("reference kernels not built (oracle/_ref)")
+    from viss_recon_shade_gb300.synth import REF_R1, REF_R2
+    ref = ref_cuda.mincline_unique(8, orbit_res, orbit_counts, index, 1e7, REF_R1, REF_R2)
+    pos = V.orbit_positions(V.OrbitConfig(orbit_res=orbit_res, orbit_counts=orbit_counts, index=index))
+    u, v, w = V.unique_uvw(pos, 30.0, ordered=True)
+    ours = torch.stack([u, v, w], 1)
+    assert ours.shape == ref.shape
+    assert torch.equal(ours.view(torch.int32), ref.view(torch.int32))

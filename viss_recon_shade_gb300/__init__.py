@@ -10,5 +10,5 @@ from .api import (ChannelBatch, DftConfig, OrbitConfig, Tuning, autotune, autotu
                   reference_d, shade_windows, tuning_candidates, unique_uvw, vis_dft, vis_dft_map, vis_dft_windowed,
                   visscal)
 from ._lib import (MASK_GEOMETRIC, MASK_NONE, MASK_REF_INTENDED, MASK_REF_QUIRK, PREC_COMPENSATED,  # noqa: F401
-                   PREC_FAST, PREC_PLAIN, RECON_MASK_GEOMETRIC, RECON_MASK_NONE, RECON_MASK_REF, VARIANT_OPTIM,
+                   PREC_F64_PHASE, PREC_FAST, PREC_PLAIN, RECON_MASK_GEOMETRIC, RECON_MASK_NONE, RECON_MASK_REF, VARIANT_OPTIM,
                    VARIANT_PLAIN, VissError)

@@ -24,7 +24,7 @@ VISS_ERR_FORMAT = -8
 
 MASK_NONE, MASK_REF_QUIRK, MASK_REF_INTENDED, MASK_GEOMETRIC = 0, 1, 2, 3
 RECON_MASK_NONE, RECON_MASK_REF, RECON_MASK_GEOMETRIC = 0, 1, 2
-PREC_PLAIN, PREC_FAST, PREC_COMPENSATED = 0, 1, 2
+PREC_PLAIN, PREC_FAST, PREC_COMPENSATED, PREC_F64_PHASE = 0, 1, 2, 3
 VARIANT_PLAIN, VARIANT_OPTIM = 0, 1
 
 

@@ -16,7 +16,7 @@ import torch
 
 from . import _lib as L
 from ._lib import (MASK_GEOMETRIC, MASK_NONE, MASK_REF_INTENDED, MASK_REF_QUIRK, PREC_COMPENSATED,  # noqa: F401
-                   PREC_FAST, PREC_PLAIN, RECON_MASK_GEOMETRIC, RECON_MASK_NONE, RECON_MASK_REF, VARIANT_OPTIM,
+                   PREC_F64_PHASE, PREC_FAST, PREC_PLAIN, RECON_MASK_GEOMETRIC, RECON_MASK_NONE, RECON_MASK_REF, VARIANT_OPTIM,
                    VARIANT_PLAIN, VissError)
 
 MOON_RADIUS_KM = 1737.4

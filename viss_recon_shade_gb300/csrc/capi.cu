@@ -150,7 +150,7 @@ static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64
   p.windexed = windexed;
   p.map = map != nullptr;
   p.X = map ? map->X : 0;
-  p.plain = cfg.precision == VISS_PREC_PLAIN;
+  p.plain = plain_precision(cfg.precision);
   p.geo = cfg.mask_mode == VISS_MASK_GEOMETRIC;
   p.ref = cfg.mask_mode == VISS_MASK_REF_QUIRK || cfg.mask_mode == VISS_MASK_REF_INTENDED;
   p.comp = cfg.precision == VISS_PREC_COMPENSATED;
@@ -275,7 +275,7 @@ static void plan_segments(RecPlan& p, const Batch& bt, const Tuning& tn) {
 static void plan_recon(RecPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64_t J, const viss_geometry* geo,
                        const Tuning& tn) {
   p.K = bt.ch.row_off[bt.ch.nch]; p.J = J;
-  p.plain = cfg.precision == VISS_PREC_PLAIN;
+  p.plain = plain_precision(cfg.precision);
   p.geo = cfg.recon_mask == VISS_RECON_MASK_GEOMETRIC;
   p.ref = cfg.recon_mask == VISS_RECON_MASK_REF;
   p.comp = cfg.precision == VISS_PREC_COMPENSATED;
@@ -295,7 +295,7 @@ static int check_cfg(const viss_dft_cfg* cfg) {
     return fail(VISS_ERR_INVALID, "mask_mode out of range");
   if (cfg->recon_mask < VISS_RECON_MASK_NONE || cfg->recon_mask > VISS_RECON_MASK_GEOMETRIC)
     return fail(VISS_ERR_INVALID, "recon_mask out of range");
-  if (cfg->precision < VISS_PREC_PLAIN || cfg->precision > VISS_PREC_COMPENSATED)
+  if (cfg->precision < VISS_PREC_PLAIN || cfg->precision > VISS_PREC_F64_PHASE)
     return fail(VISS_ERR_INVALID, "precision out of range");
   if (!(cfg->phase_scale > 0.0) || !(cfg->phase_scale <= 1.0))
     return fail(VISS_ERR_RANGE, "phase_scale must be in (0, 1]");
@@ -649,7 +649,7 @@ static int check_vis_call(const viss_dft_cfg* cfg, const viss_sky* sky, const vi
     if (!vis->shade) return fail(VISS_ERR_INVALID, "REF mask needs shade windows");
     if (cfg->res < 1) return fail(VISS_ERR_RANGE, "REF mask needs res >= 1");
   }
-  if (own_bright && cfg->trunc_brightness && cfg->precision != VISS_PREC_PLAIN)
+  if (own_bright && cfg->trunc_brightness && !plain_precision(cfg->precision))
     return fail(VISS_ERR_UNSUPPORTED, "trunc_brightness with per-channel brightness");
   if (cfg->mask_mode == VISS_MASK_GEOMETRIC && (rc = check_geo(geo, vis, cfg))) return rc;
   return VISS_OK;
@@ -894,7 +894,7 @@ int viss_imagerecon(int uvw_index, int lmnC_index, int res, float* F, const floa
   const float* ratios[4] = {thetaP0, phiP0, dtheta, dphi};
   rc = recon_impl(cfg, scale, dlmn, sky, vis, bt, nullptr, Tuning{}, viss, F, ws, p.bytes, st,
                   masked ? ratios : nullptr);
-  if (rc == VISS_OK && masked && precision != VISS_PREC_PLAIN) {
+  if (rc == VISS_OK && masked && !plain_precision(precision)) {
     // rows whose ratio arrays are not of the reference's form are rejected
     int flags[2] = {0, 0};
     p.layout(ws);

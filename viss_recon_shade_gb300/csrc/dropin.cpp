@@ -110,6 +110,36 @@ double now() {
 
 void mkdir_p(const std::string& d) { ::mkdir(d.c_str(), 0755); }
 
+// Resume (--resume 1): the reference resumes a campaign by editing start_period by
+// hand (vissGen10M_shade_optim2.cu:795); here a period whose output file already
+// holds all of its lines is skipped.  Outputs are written under a temporary name
+// and renamed when complete, so an interrupted run never leaves a partial file
+// under the final name (a partial file from elsewhere fails the line count).
+bool output_complete(const std::string& path, int ncols, int64_t rows, bool ints = false) {
+  int64_t n = -1;
+  const int rc = ints ? viss_text_read_ints(path.c_str(), ncols, nullptr, 0, &n)
+                      : viss_text_read_floats(path.c_str(), 0, ncols, nullptr, 0, &n, nullptr);
+  return rc == VISS_OK && n == rows;
+}
+
+int finish_output(const std::string& tmp, const std::string& path, int rc) {
+  if (rc != VISS_OK) {
+    std::remove(tmp.c_str());
+    return rc;
+  }
+  return std::rename(tmp.c_str(), path.c_str()) == 0 ? VISS_OK : VISS_ERR_IO;
+}
+
+int write_floats_atomic(const std::string& path, int ncols, const float* cols, int64_t stride, int64_t rows) {
+  const std::string tmp = path + ".part";
+  return finish_output(tmp, path, viss_text_write_floats(tmp.c_str(), ncols, cols, stride, rows));
+}
+
+int write_ints_atomic(const std::string& path, int ncols, const int32_t* rows_data, int64_t rows) {
+  const std::string tmp = path + ".part";
+  return finish_output(tmp, path, viss_text_write_ints(tmp.c_str(), ncols, rows_data, rows));
+}
+
 int read_col(const std::string& path, bool header, std::vector<float>& out, int64_t* hv = nullptr) {
   int64_t rows = 0, h = 0;
   int rc = viss_text_read_floats(path.c_str(), header, 1, nullptr, 0, &rows, &h);
@@ -226,8 +256,21 @@ int vissgen(const Args& a, bool tenM) {
   const bool accurate = variant == "accurate";
   const std::string outdir = tenM ? root + "/F_recon_10M/" : root + (accurate ? "/F_recon_1M_accu/" : "/F_recon_1M/");
   mkdir_p(outdir);
+  const bool resume = a.get("resume", "0") != "0";
   for (int p = start_period; p < days; ++p) {
     const double t0 = now();
+    std::string out;
+    if (tenM) {
+      const std::string suf = variant == "optim1" ? "_optim1" : variant == "optim2" ? "_optim2" : "";
+      out = outdir + "F" + std::to_string(p + 1) + "period10M" + suf + ".txt";
+    } else {
+      out = accurate ? outdir + "Ex" + std::to_string(p + 1) + dur + ".txt"
+                     : outdir + "F" + std::to_string(p + 1) + "_" + variant + ".txt";
+    }
+    if (resume && output_complete(out, 1, tenM ? J : X)) {
+      std::printf("Period %d: %s complete, skipped\n", p + 1, out.c_str());
+      continue;
+    }
     std::vector<float> uvw;
     int64_t K = 0;
     const std::string uvw_path = freq_dir + (tenM ? "updated_uvw" : "uvw") + std::to_string(p + 1) + dur + ".txt";
@@ -311,21 +354,16 @@ int vissgen(const Args& a, bool tenM) {
     const double t3 = now();
     std::vector<float> F(2 * J);
     CHECKC(cudaMemcpy(F.data(), dF.p, sizeof(float) * 2 * J, cudaMemcpyDeviceToHost));
-    std::string out;
     if (tenM) {
-      const std::string suf = variant == "optim1" ? "_optim1" : variant == "optim2" ? "_optim2" : "";
-      out = outdir + "F" + std::to_string(p + 1) + "period10M" + suf + ".txt";
       std::vector<float> re(J);
       for (int64_t j = 0; j < J; ++j) re[j] = F[2 * j];
-      CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), J, J));
+      CHECKV(write_floats_atomic(out, 1, re.data(), J, J));
     } else {
       // expanded to the fine grid: F[NX[c]-1] (vissGen1M_shade_optim1.cu:680-684,
       // vissGen1M_shade_accurate.cu:571-585 as Ex{p}frequency1M.txt)
-      out = accurate ? outdir + "Ex" + std::to_string(p + 1) + dur + ".txt"
-                     : outdir + "F" + std::to_string(p + 1) + "_" + variant + ".txt";
       std::vector<float> re(X);
       for (int64_t c = 0; c < X; ++c) re[c] = F[2 * ((int64_t)NX[c] - 1)];
-      CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
+      CHECKV(write_floats_atomic(out, 1, re.data(), X, X));
     }
     if (a.get("sidecar", "0") != "0") {
       // V (which the reference never writes) and complex F at full precision, next to the text file
@@ -412,7 +450,13 @@ int appro(const Args& a) {
   }
   const std::string outdir = root + "/F_recon_1M_appro/";
   mkdir_p(outdir);
+  const bool resume = a.get("resume", "0") != "0";
   for (int p = start_period; p < days; ++p) {
+    const std::string out = outdir + "Ex" + std::to_string(p + 1) + "frequency1M.txt";
+    if (resume && output_complete(out, 1, X)) {
+      std::printf("Period %d: %s complete, skipped\n", p + 1, out.c_str());
+      continue;
+    }
     std::vector<float> uvw;
     int64_t K = 0;
     const std::string uvw_path = dir + "uvw" + std::to_string(p + 1) + "frequency1M.txt";
@@ -465,8 +509,7 @@ int appro(const Args& a) {
       const int64_t q = (int64_t)NX[c] - 1;
       re[c] = q >= 0 && q < J ? F[2 * q] : 0.0f;
     }
-    const std::string out = outdir + "Ex" + std::to_string(p + 1) + "frequency1M.txt";
-    CHECKV(viss_text_write_floats(out.c_str(), 1, re.data(), X, X));
+    CHECKV(write_floats_atomic(out, 1, re.data(), X, X));
     std::printf("Period %d: %lld uvw -> %s\n", p + 1, (long long)K, out.c_str());
   }
   return 0;
@@ -484,12 +527,19 @@ int shade(const Args& a, const std::string& which) {
   // tid+1, so period 1 is skipped, shade10M.cu:152); shade30M: one file uvw1 -> ./shade30Mperiod1.txt
   const int first = (int)a.geti("first", which == "shade10M" ? 2 : 1);
   const int last = (int)a.geti("last", which == "shade1M" ? 130 : which == "shade10M" ? 34 : 1);
+  const bool resume = a.get("resume", "0") != "0";
   for (int p = first; p <= last; ++p) {
     const std::string in = dir + (which == "shade10M" ? "updated_uvw" : "uvw") + std::to_string(p) + dur + ".txt";
+    const std::string op = which == "shade30M" ? root + "/shade30Mperiod1.txt"
+                                               : dir + "shadeM" + std::to_string(p) + dur + ".txt";
     std::vector<float> uvw;
     int64_t K = 0;
     if (read_cols(in, which == "shade10M" ? 4 : 3, uvw, &K)) {
       std::printf("address_uvw: %s (missing, skipped)\n", in.c_str());
+      continue;
+    }
+    if (resume && output_complete(op, 4, K, true)) {
+      std::printf("period %d: %s complete, skipped\n", p, op.c_str());
       continue;
     }
     Dev<float> du, dv, dw;
@@ -505,9 +555,7 @@ int shade(const Args& a, const std::string& which) {
     CHECKV(viss_shade_windows(du.p, dv.p, dw.p, K, RES, a.getd("mean-r", 0.0), dout.p, &mean_r, ws.p, wsb, nullptr));
     std::vector<int32_t> out(4 * K);
     CHECKC(cudaMemcpy(out.data(), dout.p, sizeof(int32_t) * 4 * K, cudaMemcpyDeviceToHost));
-    const std::string op = which == "shade30M" ? root + "/shade30Mperiod1.txt"
-                                               : dir + "shadeM" + std::to_string(p) + dur + ".txt";
-    CHECKV(viss_text_write_ints(op.c_str(), 4, out.data(), K));
+    CHECKV(write_ints_atomic(op, 4, out.data(), K));
     std::printf("period %d: %lld uvw, mean r %.6g, wrote %s\n", p, (long long)K, mean_r, op.c_str());
   }
   return 0;

@@ -407,6 +407,8 @@ int launch_recon_reduce(const RecReduceParams& p, cudaStream_t st) {
 //   ph = u*l/d + v*m/d + w*(n + n_offset)/d,  x = +2 pi ph   (vissGen10M_shade.cu:169)
 // precise sincosf, register accumulator (optim1, :235-271); reference ratio
 // mask evaluated per term from r1 = M1/M2, r2 = M3/M4 (:166).
+// F64 (the FP64-phase arm of precision sweeps): the phase in FP64, reduced to
+// [-1/2, 1/2] turn in FP64, sincosf of the float angle, Kahan sums.
 struct PlainRecArgs {
   const float *u, *v, *w, *wgt, *V, *l, *m, *n;
   const float* r1;
@@ -421,20 +423,25 @@ struct PlainRecArgs {
   int res;
   float dl, dm, dn;
   float noff;
+  double noff64;
   float norm;
   double R;
   float2* out;
   int* flags;  // near-limb count (may be null)
 };
 
+template <bool F64>
 __global__ void recon_plain_kernel(const PlainRecArgs a) {
   const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= a.J) return;
   const float phiP = floorf((float)(j / a.res));
   const float thetaP = (float)j - phiP * (float)a.res;
   const float lj = a.l[j], mj = a.m[j], nj = a.n[j] + a.noff;
+  // FP64-phase arm: l/d, m/d, (n + n_offset)/d in double
+  const double ld = (double)a.l[j] / (double)a.dl, md = (double)a.m[j] / (double)a.dm;
+  const double nd = ((double)a.n[j] + a.noff64) / (double)a.dn;
   const float p2 = 2.0f * (float)kPi;
-  float fr = 0.f, fi = 0.f;
+  float fr = 0.f, fi = 0.f, cr = 0.f, ci = 0.f;
   for (int64_t k = 0; k < a.K; ++k) {
     if (a.rmask == VISS_RECON_MASK_REF) {
       const float t0 = a.r1[k], p0 = a.r2[k];
@@ -446,13 +453,23 @@ __global__ void recon_plain_kernel(const PlainRecArgs a) {
           geo_test_plain(a.l[j], a.m[j], a.n[j], a.satdir[g2], a.sat_pos + 3 * g2, a.R, a.flags))
         continue;
     }
-    const float ph = a.u[k] * lj / a.dl + a.v[k] * mj / a.dm + a.w[k] * nj / a.dn;
     float sn, cs;
-    sincosf(p2 * ph, &sn, &cs);
+    if (F64) {
+      const double t = fma((double)a.u[k], ld, fma((double)a.v[k], md, (double)a.w[k] * nd));
+      sincosf((float)((t - rint(t)) * (2.0 * kPi)), &sn, &cs);
+    } else {
+      const float ph = a.u[k] * lj / a.dl + a.v[k] * mj / a.dm + a.w[k] * nj / a.dn;
+      sincosf(p2 * ph, &sn, &cs);
+    }
     const float wg = a.wgt ? a.wgt[k] : 1.0f;
     const float yr = wg * a.V[2 * k], yi = wg * a.V[2 * k + 1];
-    fr += yr * cs - yi * sn;
-    fi += yr * sn + yi * cs;
+    if (F64) {
+      kahan_add(fr, cr, yr * cs - yi * sn);
+      kahan_add(fi, ci, yr * sn + yi * cs);
+    } else {
+      fr += yr * cs - yi * sn;
+      fi += yr * sn + yi * cs;
+    }
   }
   a.out[j] = make_float2(fr * a.norm, fi * a.norm);
 }
@@ -474,11 +491,13 @@ int launch_recon_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_
   a.res = cfg.res > 0 ? cfg.res : 1;
   a.dl = dlmn[0]; a.dm = dlmn[1]; a.dn = dlmn[2];
   a.noff = (float)cfg.n_offset;
+  a.noff64 = cfg.n_offset;
   a.norm = (float)cfg.norm;
   a.R = cfg.moon_radius_km;
   a.out = out;
   if (a.J <= 0) return VISS_OK;
-  recon_plain_kernel<<<(unsigned)((a.J + 255) / 256), 256, 0, st>>>(a);
+  if (cfg.precision == VISS_PREC_F64_PHASE) recon_plain_kernel<true><<<(unsigned)((a.J + 255) / 256), 256, 0, st>>>(a);
+  else recon_plain_kernel<false><<<(unsigned)((a.J + 255) / 256), 256, 0, st>>>(a);
   VISS_LAUNCH_CHECK("recon_plain_kernel");
   return VISS_OK;
 }

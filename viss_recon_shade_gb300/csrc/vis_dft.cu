@@ -466,6 +466,9 @@ int launch_vis_reduce(const float2* partial, int nsplit, int64_t K, float2* out,
 //   ph = u*l/d + v*m/d + w*(n-1)/d,  x = -2 pi ph  (vissGen10M_shade.cu:137-138)
 // with precise sincosf, accumulated in registers (optim1, :154-205), times the
 // trailing exp(-2 pi i (1 + n_offset) w / d) (:143).  Masks as in the tiled kernel.
+// F64 (the FP64-phase arm of precision sweeps): the whole phase
+// (u l + v m + w (n + n_offset)) / d in FP64 (the trailing factor folded in),
+// reduced to [-1/2, 1/2] turn in FP64, sincosf of the float angle, Kahan sums.
 struct PlainVisArgs {
   const float *u, *v, *w, *l, *m, *n, *bright;
   const int32_t* shade;
@@ -482,6 +485,7 @@ struct PlainVisArgs {
   float dl, dm, dn;
   float trail;  // 1 + n_offset
   double R;
+  double noff;  // n_offset (FP64-phase arm)
   float2* out;
   int* flags;  // near-limb count (may be null)
   const int32_t* widx;  // REF windows test widx[j] (NULL: j)
@@ -493,10 +497,14 @@ struct PlainVisArgs {
   int64_t X;
 };
 
+template <bool F64>
 __global__ void vis_plain_kernel(const PlainVisArgs a) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K) return;
   const float uk = a.u[k], vk = a.v[k], wk = a.w[k];
+  // FP64-phase arm: u/d, v/d, w/d in double
+  const double ud = (double)uk / (double)a.dl, vd = (double)vk / (double)a.dm, wd = (double)wk / (double)a.dn;
+  float cr = 0.f, ci = 0.f;  // Kahan compensations (FP64-phase arm)
   int4 wv = make_int4(1, 0, 0, 0);
   if ((a.mask == VISS_MASK_REF_QUIRK || a.mask == VISS_MASK_REF_INTENDED) && a.shade) {
     const int M1 = a.shade[4 * k], M2 = a.shade[4 * k + 1], M3 = a.shade[4 * k + 2], M4 = a.shade[4 * k + 3];
@@ -554,11 +562,22 @@ __global__ void vis_plain_kernel(const PlainVisArgs a) {
       if (geo_test_plain(sx, sy, sz, d1, p1, a.R, a.flags) || geo_test_plain(sx, sy, sz, d2, p2, a.R, a.flags))
         c = a.occ;
     }
-    const float ph = uk * a.l[j] / a.dl + vk * a.m[j] / a.dm + wk * (a.n[j] - 1.0f) / a.dn;
     float sn, cs;
+    if (F64) {
+      const double t = fma(ud, (double)a.l[j], fma(vd, (double)a.m[j], wd * ((double)a.n[j] + a.noff)));
+      sincosf((float)((t - rint(t)) * (-2.0 * kPi)), &sn, &cs);
+      kahan_add(ar, cr, c * cs);
+      kahan_add(ai, ci, c * sn);
+      continue;
+    }
+    const float ph = uk * a.l[j] / a.dl + vk * a.m[j] / a.dm + wk * (a.n[j] - 1.0f) / a.dn;
     sincosf(m2pi * ph, &sn, &cs);
     ar = fmaf(c, cs, ar);
     ai = fmaf(c, sn, ai);
+  }
+  if (F64) {  // the trailing factor is in the phase
+    a.out[k] = make_float2(ar, ai);
+    return;
   }
   float sn, cs;
   sincosf(m2pi * (a.trail * wk / a.dn), &sn, &cs);
@@ -585,10 +604,12 @@ int launch_vis_plain(const viss_dft_cfg& cfg, const viss_sky& sky, const viss_vi
   a.occ = cfg.occluded_value;
   a.dl = dlmn[0]; a.dm = dlmn[1]; a.dn = dlmn[2];
   a.trail = (float)(1.0 + cfg.n_offset);
+  a.noff = cfg.n_offset;
   a.R = cfg.moon_radius_km;
   a.out = out;
   if (a.K <= 0) return VISS_OK;
-  vis_plain_kernel<<<(unsigned)((a.K + 255) / 256), 256, 0, st>>>(a);
+  if (cfg.precision == VISS_PREC_F64_PHASE) vis_plain_kernel<true><<<(unsigned)((a.K + 255) / 256), 256, 0, st>>>(a);
+  else vis_plain_kernel<false><<<(unsigned)((a.K + 255) / 256), 256, 0, st>>>(a);
   VISS_LAUNCH_CHECK("vis_plain_kernel");
   return VISS_OK;
 }

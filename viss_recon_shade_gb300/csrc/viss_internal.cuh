@@ -83,6 +83,10 @@ constexpr int REC_Q = 256;                // visibilities per shared-memory tile
 constexpr int VISS_MAX_CH = VISS_MAX_CHANNELS;
 constexpr int VISS_MAX_SEG = 256;
 
+// Precisions served by the one-thread-per-item kernels (the reference's plain
+// method, and the FP64-phase arm of precision sweeps).
+inline bool plain_precision(int p) { return p == VISS_PREC_PLAIN || p == VISS_PREC_F64_PHASE; }
+
 // Geometric test: |e| below this margin is re-decided in double.
 constexpr float GEO_EPS = 2e-6f;
 
