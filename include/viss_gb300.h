@@ -341,8 +341,12 @@ VISS_API int viss_unique_uvw(const float* pos, int64_t S, int32_t nsat, int orde
 /* ---------------------------------------------------------- shade windows */
 /* Cart2SphKernel + mean radius + ShadeMatrix (shade1M.cu:62-105, 218-225).
  * out: K x 4 int32 (thetaIndS, thetaIndE, phiIndS, phiIndE), 1-based as in the shadeM files.
- * mean_r_km > 0 uses that mean radius; otherwise it is computed (double sum) and, if
- * mean_r_out (HOST) is non-NULL, returned there (the call then synchronises the stream). */
+ * mean_r_km > 0 uses that mean radius (rounded to float); otherwise it is computed as the
+ * reference computes it -- the FP32 sum of r by thrust::transform_reduce (shade1M.cu:219,
+ * same CUB reduction, same order) divided by K -- and read back to the host, so the call
+ * synchronises `stream` once.  r0 = atanf(1737.74f / (mean_r + 1737.74f)), dtheta and dphi
+ * are computed on the host as there (:222-224); the windows equal the reference's bit for
+ * bit.  mean_r_out (HOST, may be NULL) receives the mean radius used. */
 VISS_API size_t viss_shade_windows_workspace(int64_t K);
 VISS_API int viss_shade_windows(const float* u, const float* v, const float* w, int64_t K, int RES,
                        double mean_r_km, int32_t* out, double* mean_r_out, void* workspace,
