@@ -1,6 +1,8 @@
 """The drop-in programs (bin/vissGen10M_shade, vissGen1M_shade_optim1, shade10M,
 MIncline_generate_uvw_float) on a synthetic tree in the reference's layout:
-outputs land where the reference writes them and match the oracle."""
+outputs land where the reference writes them and match the oracle and, where
+the reference's kernels can run (oracle/_ref), the reference's own results on
+the same inputs (integer outputs byte for byte)."""
 import subprocess
 from pathlib import Path
 
@@ -89,6 +91,21 @@ def test_vissGen10M_shade_dropin(oracle, tmp_path):
     assert F.shape == (J,)
     assert np.abs(F - Fo.real).max() / np.abs(Fo.real).max() < 2e-5
     assert np.abs(Fs - Fo).max() / np.abs(Fo).max() < 2e-5
+    # the reference's own kernels on the inputs its main would pass them (the files as
+    # parsed, n clipped to [-1, 1] (:308), normalised windows, 1/freq weights): our F
+    # file is as close to FP64 as theirs, value for value
+    from oracle import ref_cuda
+    if ref_cuda.available():
+        import torch
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()  # noqa: E731
+        Ms = [torch.from_numpy(np.ascontiguousarray(M[:, i])).cuda() for i in range(4)]
+        args = (t(u), t(v), t(w), t(l), t(m), t(ncl))
+        viss = ref_cuda.visscal("vissGen10M_shade", K, J, res, t(FF), *args, *Ms,
+                                torch.arange(J, dtype=torch.float32, device="cuda"),
+                                torch.ones(J, dtype=torch.int32, device="cuda"))
+        Fr = ref_cuda.imagerecon("vissGen10M_shade", K, J, res, viss, *args, t(1.0 / freq), *Ms)[:, 0].cpu().numpy()
+        scale = np.abs(Fo.real).max()
+        assert np.abs(F - Fo.real).max() / scale <= 1.5 * np.abs(Fr - Fo.real).max() / scale + 1e-5
     # optim2 naming and period loop (days/start-period flags as in its main)
     run([BIN / "vissGen10M_shade_optim2", "--res", res, "--start-period", 0, "--days", 1], tmp_path)
     assert (tmp_path / "F_recon_10M" / "F1period10M_optim2.txt").exists()
