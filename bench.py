@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--no-stage1", action="store_true", help="skip the stage-1 (uvw generation) record")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-channel record")
+    ap.add_argument("--mask", choices=["geometric", "none"], default="geometric",
+                    help="occlusion mask of the DFT passes (none: every term computed, for profiling)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU work of the baseline sample")
     return ap.parse_args()
 
@@ -195,10 +197,10 @@ def choose_precision(d, pref):
     return {"fast": V.PREC_FAST, "compensated": V.PREC_COMPENSATED}[precision_name(d, pref)]
 
 
-def workload_config(wl, K, J, precision, ws):
+def workload_config(wl, K, J, precision, ws, mask="geometric"):
     """The `config` of both arms' lines (same workload, same keys and values)."""
     return {"workload": wl.name, "K": K, "J": J, "terms_per_step": int(2 * K * J), "snapshots": wl.snapshots,
-            "baselines": wl.npairs, "freq_hz": wl.freq_hz, "mask": "geometric", "precision": precision,
+            "baselines": wl.npairs, "freq_hz": wl.freq_hz, "mask": mask, "precision": precision,
             "l2": "flushed (256 MB write) before each timed step", "parallelism": f"replicas x{ws}"}
 
 
@@ -210,6 +212,8 @@ def run_ours(args, ws, rank, local):
     K, J = d["u"].numel(), d["l"].numel()
     prec = choose_precision(d, args.precision)
     cfg = V.DftConfig.geometric(precision=prec, occluded_value=0.0)
+    if args.mask == "none":
+        cfg = cfg.with_(mask=V.MASK_NONE, recon_mask=V.RECON_MASK_NONE)
     geo = dict(snap=d["snap"], pair=d["pair"], sat_pos=d["sat_pos"])
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     Vout = torch.empty(K, dtype=torch.complex64, device="cuda")
@@ -353,7 +357,7 @@ def run_ours(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fixed-point i32 phase)",
             "data": "synthetic (seeded orbit + Fibonacci sky)",
-            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws),
+            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws, args.mask),
             "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
@@ -459,7 +463,8 @@ def cpu_baseline(args, wl, d, Vout, Fout, cfg):
     l, m, n, b = (h(d[k]) for k in ("l", "m", "n", "b"))
     K, J = u.size, l.size
     thr = O.max_threads()
-    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=cfg.phase_scale, n_offset=cfg.n_offset,
+    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC if args.mask == "geometric" else O.MASK_NONE,
+                      phase_scale=cfg.phase_scale, n_offset=cfg.n_offset,
                       occluded_value=cfg.occluded_value, norm=1.0 / K)
     # calibrate, then size the sample to ~cpu_seconds
     rows = np.arange(0, K, max(1, K // 64))[:64]
@@ -548,7 +553,8 @@ def run_reference(args, ws, rank, local):
     l, m, n, b = (d[k] for k in ("l", "m", "n", "b"))
     K, J = u.size, l.size
     thr = O.max_threads()
-    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC, phase_scale=1.0, n_offset=-1.0, occluded_value=0.0, norm=1.0 / K)
+    ocfg = O.make_cfg(mask_mode=O.MASK_GEOMETRIC if args.mask == "geometric" else O.MASK_NONE, phase_scale=1.0,
+                      n_offset=-1.0, occluded_value=0.0, norm=1.0 / K)
     geo_all = O.make_geo(pos, snap, pair)
     # calibrate on 4 rows a thread, then size the sample to ~cpu_seconds / 4 per step
     rows = np.linspace(0, K - 1, 4 * thr).astype(np.int64)
@@ -581,11 +587,11 @@ def run_reference(args, ws, rank, local):
             "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded orbit + Fibonacci sky)",
             "impl": "reference",
-            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws),
+            "config": workload_config(wl, K, J, precision_name(d, args.precision), ws, args.mask),
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": thr, "kind": "port",
                              "sample": f"per step {nr} visibilities x {J} pixels + {np_} pixels x {K} visibilities "
                                        f"({nr * J + np_ * K:.3g} terms), FP64 restatement of visscal/imagerecon "
-                                       "(oracle/viss_oracle.cpp) with the geometric mask, OpenMP on every host "
+                                       f"(oracle/viss_oracle.cpp) with the {args.mask} mask, OpenMP on every host "
                                        "thread"},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if not args.no_ref_cuda:
