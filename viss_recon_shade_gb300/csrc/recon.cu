@@ -57,7 +57,7 @@ struct RecSmem {
   float4 r1[Q];
   float4 rf[COMP ? Q : 1];
   int4 win[RM == RM_REF ? Q : 1];
-  int pk[RM == RM_GEO ? Q : 1];
+  uint32_t pm[RM == RM_GEO ? Q : 1];   // the row's two satellites as bits of its snapshot's satellites
   int snap[RM == RM_GEO ? Q : 1];
   int runend[RM == RM_GEO ? Q : 1];
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
@@ -96,9 +96,9 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
     if (RM == RM_REF) { const int2 qr = p.pqr[pos]; PP[i] = qr.x; TP[i] = qr.y; }
     sm.acc[tid * REC_TJ + i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  bool valid[REC_TJ];
+  unsigned valid = 0;  // bit i: pixel i of this thread is a real pixel
 #pragma unroll
-  for (int i = 0; i < REC_TJ; ++i) valid[i] = j0 + i < p.J;
+  for (int i = 0; i < REC_TJ; ++i) valid |= (j0 + i < p.J ? 1u : 0u) << i;
   const int64_t jfirst = pb * REC_PIX;
   int64_t jlast = jfirst + REC_PIX - 1;
   if (jlast > p.J - 1) jlast = p.J - 1;
@@ -160,7 +160,8 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
           sm.r1[off] = p.rows1[k];
           if (COMP) sm.rf[off] = p.rowsf[k];
           const int sn = sat_gm(pk[h]) / p.nsat;
-          sm.pk[off] = pk[h];
+          const int g0 = sn * p.nsat;
+          sm.pm[off] = (1u << (sat_gm(pk[h]) - g0)) | (1u << (sat_gn(pk[h]) - g0));
           sm.snap[off] = sn;
           atomicMin(&sm.srange[0], sn);
           atomicMax(&sm.srange[1], sn);
@@ -217,8 +218,9 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         for (int i = 0; i < REC_TJ; ++i) {
           const float4 g = __ldg(p.pgeo + j0 + i);
           const float d = fmaf(g.x, c0.x, fmaf(g.y, c0.y, g.z * c0.z));
-          all_vis &= (!valid[i]) || d < c1;
-          all_occ &= (!valid[i]) || d > c0.w;
+          const bool v = (valid >> i) & 1u;
+          all_vis &= !v || d < c1;
+          all_occ &= !v || d > c0.w;
         }
         const bool wocc = __all_sync(0xffffffffu, all_occ);
         const bool wvis = __all_sync(0xffffffffu, all_vis);
@@ -248,17 +250,17 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
               const float4 d = cached ? sm.sat[(sn - s_lo) * p.nsat + sat] : __ldg(p.satdir + g0 + sat);
               const float e = fmaf(g.x, d.x, fmaf(g.y, d.y, fmaf(g.z, d.z, d.w)));
               bool occ = e < 0.f;
-              if (fabsf(e) < GEO_EPS && valid[i]) occ = geo_exact_pix(p, __float_as_int(g.w), g0 + sat);
+              if (fabsf(e) < GEO_EPS && ((valid >> i) & 1u)) occ = geo_exact_pix(p, __float_as_int(g.w), g0 + sat);
               bits[i] |= (occ ? 1u : 0u) << sat;
             }
           }
+#pragma unroll 2
           for (int rr = r; rr < re; ++rr) {
             const int4 r0 = sm.r0[rr];
             const float4 r1 = sm.r1[rr];
             float4 rf = make_float4(0.f, 0.f, 0.f, 0.f);
             if (COMP) rf = sm.rf[rr];
-            const int pk = sm.pk[rr];
-            const uint32_t pm = (1u << (sat_gm(pk) - g0)) | (1u << (sat_gn(pk) - g0));
+            const uint32_t pm = sm.pm[rr];
 #pragma unroll
             for (int i = 0; i < REC_TJ; ++i) {
               const float c = (bits[i] & pm) ? 0.f : r1.w;
