@@ -232,7 +232,8 @@ static void plan_segments(RecPlan& p, const Batch& bt, const Tuning& tn) {
   const int nch = bt.ch.nch;
   // items per CTA: many short segments balance blocks whose pixels the Moon hides for
   // different parts of the orbit (10 MHz recon: 4 items 191 ms, 8 176 ms, 32 167 ms, 64 165 ms)
-  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 64) * planned_ctas(tn, VISS_REC_MINB);
+  // resident CTAs: VISS_REC_MINB for the geometric kernel, one more for the others (recon.cu)
+  const int64_t target = (tn.rec_items > 0 ? tn.rec_items : 64) * planned_ctas(tn, p.geo ? VISS_REC_MINB : VISS_REC_MINB + 1);
   int64_t L = p.npb > 0 ? (p.K * p.npb + target - 1) / target : p.K;
   L = round_up(L > unit ? L : unit, unit);
   auto count = [&](int64_t len) {

@@ -327,8 +327,15 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
 // Persistent: grid = resident CTAs; each CTA takes the next work item (segment,
 // pixel block) from an atomic counter until none are left.  The counter is
 // reset by the host before the launch; no CTA waits on another.
+// Resident CTAs per SM the instances are compiled for.  The unmasked and REF-mask ones
+// fit in 64 registers (a few spills in the REF one), and a fourth CTA hides their tile
+// barriers better (10 MHz recon: unmasked 168.0 -> 162.4 ms, REF windows 168.3 -> 161.2);
+// the geometric one needs 80 (at 64 it spills in its term loops: 163 -> 177 ms).
+template <int RM>
+constexpr int rec_min_blocks() { return RM != RM_GEO ? VISS_REC_MINB + 1 : VISS_REC_MINB; }
+
 template <int RM, bool COMP, int Q>
-__global__ void __launch_bounds__(REC_THREADS, VISS_REC_MINB) recon_fast_kernel(const ReconParams p) {
+__global__ void __launch_bounds__(REC_THREADS, rec_min_blocks<RM>()) recon_fast_kernel(const ReconParams p) {
   __shared__ RecSmem<RM, COMP, Q> sm;
   __shared__ int s_item;
   const bool frac = __ldg(p.flags + FLAG_FRAC) != 0;
