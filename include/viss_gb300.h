@@ -254,7 +254,8 @@ typedef struct viss_tuning {
   int32_t rec_items;         /* recon work items per persistent CTA the row segments aim at (0: 64) */
   int32_t tile;              /* tile shapes: bit 0 vis sky tiles of 256 pixels (else 512),
                                 bit 1 recon row tiles of 128 visibilities, bit 3 of 256
-                                (else 512; bit 2 asks for 512 explicitly) */
+                                (else 512, 1,024 with the geometric mask at FAST precision;
+                                bit 2 asks for that default explicitly) */
 } viss_tuning;
 
 VISS_API size_t viss_vis_dft_batch_workspace(const viss_dft_cfg* cfg, const viss_batch* batch, int64_t K, int64_t J,

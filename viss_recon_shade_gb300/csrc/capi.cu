@@ -527,10 +527,10 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
   rp.K = vis.K; rp.J = sky.J;
   rp.res = cfg.res > 0 ? cfg.res : 1; rp.nsat = geo ? geo->nsat : 1; rp.R = cfg.moon_radius_km;
   rp.recon_mask = cfg.recon_mask;
-  // Row tiles: as asked, else 512 rows.  Geometric recon, 512 against 256 rows:
-  // 10 MHz 167.8 / 169.9 ms, its 49,152-pixel case 12.38 / 12.58 ms, 30 MHz
-  // 2,541 / 2,579 ms (longer tiles drop hidden rows and meet at barriers less
-  // often); unmasked 168.3 / 168.2 ms.
+  // Row tiles: as asked, else 512 rows (1,024 with the geometric mask, recon.cu).
+  // Geometric recon, 512 against 256 rows: 10 MHz 167.8 / 169.9 ms, its 49,152-pixel
+  // case 12.38 / 12.58 ms, 30 MHz 2,541 / 2,579 ms (longer tiles drop hidden rows and
+  // meet at barriers less often); unmasked 168.3 / 168.2 ms.
   if ((tn.tile >> 1) & 1) rp.row_tile = 1;
   else if ((tn.tile >> 3) & 1) rp.row_tile = 0;
   else rp.row_tile = 2;

@@ -5,7 +5,8 @@
 //
 // A work item is REC_PIX = 1024 pixels (4 per thread, fixed-point coordinates
 // in registers) against one segment of visibility rows of one channel, streamed
-// through shared memory in tiles of 2 REC_Q rows (REC_Q or REC_Q / 2 on request).
+// through shared memory in tiles of 2 REC_Q rows, 4 REC_Q with the geometric mask and
+// no compensation (REC_Q or REC_Q / 2 on request).
 // The phase of y_k is folded into the
 // row's fixed-point bias (y e^{ix} = |y| e^{i(x + arg y)}), so a term is the
 // same as in the vis kernel: 3 IMAD [+3 FFMA fractional uvw] [+3 FFMA
@@ -48,7 +49,7 @@ __device__ __forceinline__ void rec_term(const int4& r0, const float4& r1, const
 }
 
 constexpr int RM_NONE = 0, RM_REF = 1, RM_GEO = 2;
-constexpr int REC_SAT_CACHE = 1024;  // satellite directions cached per tile (float4)
+constexpr int REC_SAT_CACHE = 512;   // satellite directions cached per tile (float4)
 constexpr int REC_CONE_CACHE = 128;  // snapshot cones cached per tile
 
 template <int RM, bool COMP, int Q>
@@ -361,15 +362,21 @@ static void launch_tile(const ReconParams& p, int ctas_per_sm, cudaStream_t st) 
   recon_fast_kernel<RM, COMP, Q><<<g, REC_THREADS, 0, st>>>(p);
 }
 
-// Row tiles of 2 REC_Q visibilities (the default), REC_Q or REC_Q / 2 (tuning).
+// Row tiles of 2 REC_Q visibilities (the default; 4 REC_Q for the geometric mask without
+// compensation), REC_Q or REC_Q / 2 (tuning).  Longer geometric tiles meet at the block
+// barrier half as often and drop more hidden rows per load (10 MHz recon 163.0 -> 161.1
+// ms; the satellite cache is halved to keep three CTAs per SM: 37 snapshots of 8
+// satellites fit).  The compensated instance keeps 2 REC_Q: at 4 REC_Q its shared
+// memory would leave two CTAs per SM.
 template <int RM>
 static void launch_rm(const ReconParams& p, int ctas_per_sm, bool comp, cudaStream_t st) {
+  constexpr int QD = RM == RM_GEO ? 4 * REC_Q : 2 * REC_Q;
   if (p.row_tile == 1) {
     if (comp) launch_tile<RM, true, REC_Q / 2>(p, ctas_per_sm, st);
     else launch_tile<RM, false, REC_Q / 2>(p, ctas_per_sm, st);
   } else if (p.row_tile == 2) {
     if (comp) launch_tile<RM, true, 2 * REC_Q>(p, ctas_per_sm, st);
-    else launch_tile<RM, false, 2 * REC_Q>(p, ctas_per_sm, st);
+    else launch_tile<RM, false, QD>(p, ctas_per_sm, st);
   } else {
     if (comp) launch_tile<RM, true, REC_Q>(p, ctas_per_sm, st);
     else launch_tile<RM, false, REC_Q>(p, ctas_per_sm, st);

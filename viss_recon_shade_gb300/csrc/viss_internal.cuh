@@ -300,7 +300,7 @@ struct ReconParams {
   int64_t seg_lo[VISS_MAX_SEG], seg_hi[VISS_MAX_SEG];
   int seg_ch[VISS_MAX_SEG], seg_slot[VISS_MAX_SEG];   // slot -1: the segment writes F directly
   float ch_norm[VISS_MAX_CH];
-  int row_tile;           // visibility rows per tile: 0 REC_Q, 1 REC_Q / 2, 2 2 * REC_Q
+  int row_tile;           // visibility rows per tile: 0 REC_Q, 1 REC_Q / 2, 2 2 * REC_Q (geometric, not compensated: 4 * REC_Q)
 };
 
 // Per-channel sum of partial slots (channels split into several segments).
