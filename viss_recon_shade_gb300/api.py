@@ -246,7 +246,7 @@ class Tuning:
     vis_split: int = 0
     rec_items: int = 0
     tile: int = 0  # bit 0: vis sky tiles of 256 pixels (else 512); bit 1 / 3: recon row tiles of 128 / 256
-    # rows (else 512; bit 2 asks for 512 explicitly)
+    # rows (else 512, 1,024 with the geometric mask at FAST precision; bit 2 asks for that default)
 
     def c(self) -> L.Tuning:
         return L.Tuning(int(self.ctas_per_sm), int(self.vis_split), int(self.rec_items), int(self.tile))
