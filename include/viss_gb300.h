@@ -219,8 +219,9 @@ VISS_API int viss_workspace_flags(const void* workspace, int32_t* flags, void* s
 /* No counterpart in the reference (its masks are the REF windows of shade1M.cu:73-105).
  * GEOMETRIC mask: how many occlusion tests of the completed pass fell within 2e-6 (in the
  * cosine of the angle to the limb) of the Moon's limb and were decided in double from the
- * original inputs instead (count of (visibility, pixel, satellite) tests; the fast kernels
- * test fewer terms than the plain ones, as they drop blocks the cones decide).  Reads the
+ * original inputs instead (count of occlusion tests; the plain kernels test every
+ * (visibility, pixel, satellite), the fast ones drop blocks the cones decide and the fast
+ * vis kernel tests a (pixel, satellite) pair once per block of 1,024 visibilities).  Reads the
  * workspace like viss_workspace_flags (synchronises `stream`). */
 VISS_API int viss_workspace_limb_count(const void* workspace, int64_t* count, void* stream);
 

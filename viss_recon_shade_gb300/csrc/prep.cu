@@ -362,7 +362,9 @@ struct RowMember {
   }
 };
 
-// One cone per padded block of VIS_ROWS rows, over the block's real rows.
+// One cone per padded block of VIS_ROWS rows, over the block's real rows; the
+// unused lanes of cone[1] get the range of satellite indices those rows use
+// (y: the first, z: how many, as int bits; z = 0 for an empty block).
 __global__ void rowblock_cones_kernel(const int* rowsat, const float4* satdir, const ChannelRows ch, float4* cones) {
   const int64_t b = blockIdx.x;
   int c = 0;
@@ -371,6 +373,24 @@ __global__ void rowblock_cones_kernel(const int* rowsat, const float4* satdir, c
   if (cnt > VIS_ROWS) cnt = VIS_ROWS;
   if (cnt < 0) cnt = 0;
   cone_block(satdir, 2 * cnt, RowMember{rowsat, b * VIS_ROWS}, cones + 2 * b);
+  __shared__ int rlo[32], rhi[32];
+  int lo = 0x7fffffff, hi = -1;
+  for (int64_t i = threadIdx.x; i < cnt; i += blockDim.x) {
+    const int pk = rowsat[b * VIS_ROWS + i];
+    lo = min(lo, min(sat_gm(pk), sat_gn(pk)));
+    hi = max(hi, max(sat_gm(pk), sat_gn(pk)));
+  }
+  for (int o = 16; o; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+  }
+  if ((threadIdx.x & 31) == 0) { rlo[threadIdx.x >> 5] = lo; rhi[threadIdx.x >> 5] = hi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { lo = min(lo, rlo[w]); hi = max(hi, rhi[w]); }
+    cones[2 * b + 1].y = __int_as_float(hi >= lo ? lo : 0);
+    cones[2 * b + 1].z = __int_as_float(hi >= lo ? hi - lo + 1 : 0);
+  }
 }
 
 int launch_prep_rowblock_cones(const int* rowsat, const float4* satdir, const ChannelRows& ch, int64_t nblocks,

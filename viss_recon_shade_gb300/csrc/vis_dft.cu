@@ -132,6 +132,7 @@ struct VisSmem {
   int4 win[REF ? VIS_ROWS : 1];   // the block's REF windows, read in masked tiles only
   int wcnt[VIS_THREADS / 32][2];
   float4 acc[VIS_ROWS];           // running totals (re, im) and their Kahan compensation per visibility
+  uint32_t sbits[GEO ? VIS_SAT_WORDS : 1];  // [satellite][word]: bit b = mixed pixel 32*word + b occluded
 };
 
 template <int MASK, bool FRAC, bool COMP, int P>
@@ -186,6 +187,7 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP,
     cone0 = p.cones[2 * rb];
     cone1 = p.cones[2 * rb + 1];
   }
+  const int g_lo = __float_as_int(cone1.y), g_span = __float_as_int(cone1.z);  // the rows' satellites
   const float occ_val = p.occ_val;
 
   const int64_t jb = (int64_t)split * p.jchunk;
@@ -327,7 +329,55 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP,
         }
       }
     }
-    if (GEO && nmix > 0) {
+    const int nwd = (nmix + 31) >> 5;
+    if (GEO && nmix > 0 && g_span > 0 && g_span <= VIS_ROWS && g_span * nwd <= VIS_SAT_WORDS) {
+      // Each (mixed pixel, satellite) decided once for the tile: span x nmix
+      // tests instead of up to 2 x VIS_ROWS x nmix.  A warp per satellite, a
+      // ballot per 32-pixel word.
+      for (int s = warp; s < g_span; s += VIS_THREADS / 32) {
+        const float4 d = __ldg(p.satdir + g_lo + s);
+        for (int wd = 0; wd < nwd; ++wd) {
+          const int mi = 32 * wd + lane;
+          const bool occ = mi < nmix && geo_test(s_geo[P - 1 - mi], d, g_lo + s, p);
+          const unsigned bits = __ballot_sync(0xffffffffu, occ);
+          if (lane == 0) sm.sbits[s * nwd + wd] = bits;
+        }
+      }
+      // word offsets of each row's two satellites (padding rows, outside the
+      // block's range, read satellite g_lo; their sums are never stored)
+      int so[VIS_TK];
+#pragma unroll
+      for (int i = 0; i < VIS_TK; ++i) {
+        const int pk = __ldg(p.rowsat + row0 + tid + i * VIS_THREADS);
+        int sa = sat_gm(pk) - g_lo, sb = sat_gn(pk) - g_lo;
+        if ((unsigned)sa >= (unsigned)g_span) sa = 0;
+        if ((unsigned)sb >= (unsigned)g_span) sb = 0;
+        so[i] = sa * nwd | (sb * nwd) << 16;
+      }
+      __syncthreads();
+      for (int wd = 0; wd < nwd; ++wd) {
+        unsigned ob[VIS_TK];  // occluded from either satellite, 32 pixels per word
+#pragma unroll
+        for (int i = 0; i < VIS_TK; ++i) ob[i] = sm.sbits[(so[i] & 0xffff) + wd] | sm.sbits[(so[i] >> 16) + wd];
+        const int nb = min(32, nmix - 32 * wd);
+        for (int bi = 0; bi < nb; ++bi) {
+          const int pi = P - 1 - (32 * wd + bi);
+          const int4 a = s_p0[pi];
+          int4 b = make_int4(0, 0, 0, 0);
+          float4 lo = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (FRAC) b = s_p1[pi];
+          if (COMP) lo = s_lo[pi];
+          const float c0 = __int_as_float(a.w);
+#pragma unroll
+          for (int i = 0; i < VIS_TK; ++i) {
+            const float c = (ob[i] >> bi) & 1u ? occ_val : c0;
+            if (c != 0.f)
+              vis_term<FRAC, COMP>(a, b, lo, c, U[i], V[i], W[i], FU[i], FV[i], FW[i], BI[i], UF[i], VF[i], WF[i],
+                                   tr[i], ti[i]);
+          }
+        }
+      }
+    } else if (GEO && nmix > 0) {
       int gm[VIS_TK], gn[VIS_TK];
 #pragma unroll
       for (int i = 0; i < VIS_TK; ++i) {

@@ -64,6 +64,9 @@ constexpr int VIS_THREADS = 256;
 constexpr int VIS_TK = 4;                 // visibilities per thread
 constexpr int VIS_ROWS = VIS_THREADS * VIS_TK;
 constexpr int VIS_P = 512;                // pixels per shared-memory tile
+// Geometric mask: occlusion bits of a tile's straddling pixels against every
+// satellite its rowblock uses, in shared memory (satellites x 32-pixel words).
+constexpr int VIS_SAT_WORDS = 5120;
 constexpr int REC_THREADS = 256;
 constexpr int REC_TJ = 4;                 // pixels per thread
 constexpr int REC_PIX = REC_THREADS * REC_TJ;
@@ -238,7 +241,7 @@ struct VisParams {
   const float4* rowsf;
   const int4* win;
   const float4* satdir;   // [S*nsat] {p_hat, cos_alpha}
-  const float4* cones;    // [nrb*2]
+  const float4* cones;    // [nrb*2]; cones[2b+1].y/.z: the block's first satellite and span (int bits)
   const float* l;
   const float* m;
   const float* n;
