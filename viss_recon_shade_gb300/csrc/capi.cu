@@ -184,7 +184,7 @@ struct RecPlan {
   bool geo = false, ref = false, comp = false, plain = false;
   int4 *pix0 = nullptr, *pix1 = nullptr, *rows0 = nullptr, *win = nullptr;
   float4 *rows1 = nullptr, *plo = nullptr, *pgeo = nullptr, *rowsf = nullptr, *satdir = nullptr, *scones = nullptr;
-  float4* bcones = nullptr;
+  float4 *bcones = nullptr, *wcones = nullptr;
   int* rowsat = nullptr;
   int2* pqr = nullptr;
   float2* partial = nullptr;
@@ -217,7 +217,12 @@ struct RecPlan {
       if (geo) rowsat = c.take<int>(Kpad);
       if (comp) rowsf = c.take<float4>(Kpad);
       if (ref) win = c.take<int4>(Kpad);
-      if (geo) { satdir = c.take<float4>(nsd); scones = c.take<float4>(2 * S); bcones = c.take<float4>(2 * npb); }
+      if (geo) {
+        satdir = c.take<float4>(nsd);
+        scones = c.take<float4>(2 * S);
+        bcones = c.take<float4>(2 * npb);
+        wcones = c.take<float4>(2 * npb * (REC_THREADS / 32));
+      }
       if (nslot > 0) partial = c.take<float2>((size_t)nslot * J);
     }
     bytes = c.size();
@@ -514,11 +519,13 @@ int recon_impl(const viss_dft_cfg& cfg, const double scale[3], const float dlmn[
     if ((rc = launch_prep_satdir(geo->sat_pos, p.nsd, cfg.moon_radius_km, p.satdir, st))) return rc;
     if ((rc = launch_prep_snapshot_cones(p.satdir, geo->S, geo->nsat, p.scones, st))) return rc;
     if ((rc = launch_prep_block_cones(p.pgeo, sky.J, REC_PIX, p.npb, p.bcones, st))) return rc;
+    if ((rc = launch_prep_block_cones(p.pgeo, sky.J, 32 * REC_TJ, p.npb * (REC_THREADS / 32), p.wcones, st)))
+      return rc;
   }
   ReconParams rp{};
   rp.pix0 = p.pix0; rp.pix1 = p.pix1; rp.plo = p.plo; rp.pgeo = p.pgeo; rp.pqr = p.pqr;
   rp.rows0 = p.rows0; rp.rows1 = p.rows1; rp.rowsat = p.rowsat; rp.rowsf = p.rowsf; rp.win = p.win;
-  rp.satdir = p.satdir; rp.scones = p.scones; rp.bcones = p.bcones;
+  rp.satdir = p.satdir; rp.scones = p.scones; rp.bcones = p.bcones; rp.wcones = p.wcones;
   rp.l = sky.l; rp.m = sky.m; rp.n = sky.n; rp.sat_pos = geo ? geo->sat_pos : nullptr;
   rp.flags = p.flags;
   rp.perm = p.perm;

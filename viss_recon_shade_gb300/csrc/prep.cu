@@ -283,7 +283,8 @@ int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satd
 // alpha_i): axis c = normalise(sum -p_hat_i), rho = max angle(c, -p_hat_i).
 // A pixel s_hat with s_hat.c > cos(alpha_min - rho - eps) is occluded for every
 // satellite of the set; with s_hat.c < cos(alpha_max + rho + eps) it is visible
-// from every one.  cone[0] = {c, cos_occ}, cone[1] = {cos_vis, -, -, -}.
+// from every one.  cone[0] = {c, cos_occ}, cone[1] = {cos_vis, sin_occ, sin_vis, -}
+// (the sines of the two angles, 0 where the cosine is the 2 / -2 of "never").
 // Degenerate sets (a satellite at the origin) get cos_occ = 2, cos_vis = -2.
 // Block-wide: one block per cone; members enumerated by `member(i)` -> satdir index.
 template <class Member>
@@ -338,18 +339,18 @@ __device__ void cone_block(const float4* satdir, int64_t count, Member member, f
     double mc = 2.0, a0 = 10.0, a1 = -1.0;
     for (int w = 0; w < nw; ++w) { mc = fmin(mc, red[0][w]); a0 = fmin(a0, red[1][w]); a1 = fmax(a1, red[2][w]); }
     const double eps = 1e-5;
-    float cos_occ = 2.f, cos_vis = -2.f;
+    float cos_occ = 2.f, cos_vis = -2.f, sin_occ = 0.f, sin_vis = 0.f;
     if (!degen_s && count > 0) {
       const double rho = acos(fmin(1.0, fmax(-1.0, mc)));
       const double lo = a0 - rho - eps, hi = a1 + rho + eps;
-      if (lo > 0) cos_occ = (float)cos(lo);
-      if (hi < kPi) cos_vis = (float)cos(hi);
+      if (lo > 0) { cos_occ = (float)cos(lo); sin_occ = (float)sin(lo); }
+      if (hi < kPi) { cos_vis = (float)cos(hi); sin_vis = (float)sin(hi); }
       // widen by float rounding of the test s_hat . c
       if (cos_occ <= 1.f) cos_occ = fminf(2.f, cos_occ + 1e-6f);
       if (cos_vis >= -1.f) cos_vis = cos_vis - 1e-6f;
     }
     out[0] = make_float4((float)axis[0], (float)axis[1], (float)axis[2], cos_occ);
-    out[1] = make_float4(cos_vis, 0.f, 0.f, 0.f);
+    out[1] = make_float4(cos_vis, sin_occ, sin_vis, 0.f);
   }
 }
 
@@ -363,8 +364,9 @@ struct RowMember {
 };
 
 // One cone per padded block of VIS_ROWS rows, over the block's real rows; the
-// unused lanes of cone[1] get the range of satellite indices those rows use
-// (y: the first, z: how many, as int bits; z = 0 for an empty block).
+// sines in cone[1] (which the vis kernel does not use) are replaced by the range
+// of satellite indices those rows use (y: the first, z: how many, as int bits;
+// z = 0 for an empty block).
 __global__ void rowblock_cones_kernel(const int* rowsat, const float4* satdir, const ChannelRows ch, float4* cones) {
   const int64_t b = blockIdx.x;
   int c = 0;

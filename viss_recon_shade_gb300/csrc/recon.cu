@@ -63,6 +63,7 @@ struct RecSmem {
   int runend[RM == RM_GEO ? Q : 1];
   float4 sat[RM == RM_GEO ? REC_SAT_CACHE : 1];
   float4 cone[RM == RM_GEO ? 2 * REC_CONE_CACHE : 1];
+  float4 wcap[RM == RM_GEO ? 2 * (REC_THREADS / 32) : 1];  // each warp's patch: {axis, cos r}, {sin r}
   int srange[2];
   int wkeep[(REC_THREADS / 32) * ((Q + REC_THREADS - 1) / REC_THREADS)];
   float4 acc[REC_PIX];            // running totals (re, im) and their Kahan compensation per pixel
@@ -111,6 +112,10 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
   if (RM == RM_GEO) {
     bc0 = __ldg(p.bcones + 2 * pb);
     bsin = __ldg(p.bcones + 2 * pb + 1).x;
+    // this warp's patch cap (read and written by this warp only)
+    if ((tid & 31) < 2)
+      sm.wcap[2 * (tid >> 5) + (tid & 31)] = __ldg(p.wcones + 2 * (pb * (REC_THREADS / 32) + (tid >> 5)) + (tid & 31));
+    __syncwarp();
   }
 
   for (int64_t tile = kb; tile < ke; tile += Q) {
@@ -213,18 +218,33 @@ __device__ __forceinline__ void recon_body(const ReconParams& p, RecSmem<RM, COM
         const int re = sm.runend[r];
         const int sn = sm.snap[r];
         const float4 c0 = cached ? sm.cone[2 * (sn - s_lo)] : __ldg(p.scones + 2 * (int64_t)sn);
-        const float c1 = cached ? sm.cone[2 * (sn - s_lo) + 1].x : __ldg(p.scones + 2 * (int64_t)sn + 1).x;
-        bool all_vis = true, all_occ = true;
-#pragma unroll
-        for (int i = 0; i < REC_TJ; ++i) {
-          const float4 g = __ldg(p.pgeo + j0 + i);
-          const float d = fmaf(g.x, c0.x, fmaf(g.y, c0.y, g.z * c0.z));
-          const bool v = (valid >> i) & 1u;
-          all_vis &= !v || d < c1;
-          all_occ &= !v || d > c0.w;
+        const float4 c1 = cached ? sm.cone[2 * (sn - s_lo) + 1] : __ldg(p.scones + 2 * (int64_t)sn + 1);
+        // The warp's patch cap {a, r} against the snapshot's cones (warp-uniform):
+        // all hidden when angle(a, c) + r < alpha_occ, i.e. a.c > cos(alpha_occ - r);
+        // all visible when angle(a, c) - r > alpha_vis, i.e. a.c < cos(alpha_vis + r)
+        // (alpha_vis + r < pi).  Margins of 1e-5 in the cosine; what the cap leaves
+        // open the per-pixel vote decides, so the decisions are the vote's.
+        const float4 wc = sm.wcap[2 * (tid >> 5)];
+        const float ws = sm.wcap[2 * (tid >> 5) + 1].x;
+        const float dw = fmaf(wc.x, c0.x, fmaf(wc.y, c0.y, wc.z * c0.z));
+        bool wocc = false, wvis = false;
+        if (wc.w >= -1.f) {
+          wocc = c0.w <= 1.f && c0.w < wc.w && dw > fmaf(c0.w, wc.w, c1.y * ws) + 1e-5f;
+          wvis = c1.x >= -1.f && fmaf(c1.z, wc.w, c1.x * ws) > 0.f && dw < fmaf(c1.x, wc.w, -c1.z * ws) - 1e-5f;
         }
-        const bool wocc = __all_sync(0xffffffffu, all_occ);
-        const bool wvis = __all_sync(0xffffffffu, all_vis);
+        if (!wocc && !wvis) {
+          bool all_vis = true, all_occ = true;
+#pragma unroll
+          for (int i = 0; i < REC_TJ; ++i) {
+            const float4 g = __ldg(p.pgeo + j0 + i);
+            const float d = fmaf(g.x, c0.x, fmaf(g.y, c0.y, g.z * c0.z));
+            const bool v = (valid >> i) & 1u;
+            all_vis &= !v || d < c1.x;
+            all_occ &= !v || d > c0.w;
+          }
+          wocc = __all_sync(0xffffffffu, all_occ);
+          wvis = __all_sync(0xffffffffu, all_vis);
+        }
         if (wocc) { r = re; continue; }
         if (wvis) {
 #pragma unroll 2

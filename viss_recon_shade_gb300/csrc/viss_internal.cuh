@@ -282,6 +282,7 @@ struct ReconParams {
   const float4* satdir;
   const float4* scones;   // [S*2] per-snapshot cones
   const float4* bcones;   // [npb*2] bounding cone of each pixel block: {axis, cos r}, {sin r}
+  const float4* wcones;   // [npb*2*REC_THREADS/32] the same per warp's patch of 32*REC_TJ positions
   const float* l;
   const float* m;
   const float* n;
