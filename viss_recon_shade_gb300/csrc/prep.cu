@@ -286,6 +286,24 @@ int launch_prep_satdir(const float* sat_pos, int64_t nsd, double R, float4* satd
 // from every one.  cone[0] = {c, cos_occ}, cone[1] = {cos_vis, sin_occ, sin_vis, -}
 // (the sines of the two angles, 0 where the cosine is the 2 / -2 of "never").
 // Degenerate sets (a satellite at the origin) get cos_occ = 2, cos_vis = -2.
+// From the axis, the smallest cosine to it (mc) and the cone-angle range [a0, a1].
+__device__ void cone_write(const double* axis, double mc, double a0, double a1, bool degen, int64_t count,
+                           float4* out) {
+  const double eps = 1e-5;
+  float cos_occ = 2.f, cos_vis = -2.f, sin_occ = 0.f, sin_vis = 0.f;
+  if (!degen && count > 0) {
+    const double rho = acos(fmin(1.0, fmax(-1.0, mc)));
+    const double lo = a0 - rho - eps, hi = a1 + rho + eps;
+    if (lo > 0) { cos_occ = (float)cos(lo); sin_occ = (float)sin(lo); }
+    if (hi < kPi) { cos_vis = (float)cos(hi); sin_vis = (float)sin(hi); }
+    // widen by float rounding of the test s_hat . c
+    if (cos_occ <= 1.f) cos_occ = fminf(2.f, cos_occ + 1e-6f);
+    if (cos_vis >= -1.f) cos_vis = cos_vis - 1e-6f;
+  }
+  out[0] = make_float4((float)axis[0], (float)axis[1], (float)axis[2], cos_occ);
+  out[1] = make_float4(cos_vis, sin_occ, sin_vis, 0.f);
+}
+
 // Block-wide: one block per cone; members enumerated by `member(i)` -> satdir index.
 template <class Member>
 __device__ void cone_block(const float4* satdir, int64_t count, Member member, float4* out) {
@@ -338,19 +356,7 @@ __device__ void cone_block(const float4* satdir, int64_t count, Member member, f
   if (tid == 0) {
     double mc = 2.0, a0 = 10.0, a1 = -1.0;
     for (int w = 0; w < nw; ++w) { mc = fmin(mc, red[0][w]); a0 = fmin(a0, red[1][w]); a1 = fmax(a1, red[2][w]); }
-    const double eps = 1e-5;
-    float cos_occ = 2.f, cos_vis = -2.f, sin_occ = 0.f, sin_vis = 0.f;
-    if (!degen_s && count > 0) {
-      const double rho = acos(fmin(1.0, fmax(-1.0, mc)));
-      const double lo = a0 - rho - eps, hi = a1 + rho + eps;
-      if (lo > 0) { cos_occ = (float)cos(lo); sin_occ = (float)sin(lo); }
-      if (hi < kPi) { cos_vis = (float)cos(hi); sin_vis = (float)sin(hi); }
-      // widen by float rounding of the test s_hat . c
-      if (cos_occ <= 1.f) cos_occ = fminf(2.f, cos_occ + 1e-6f);
-      if (cos_vis >= -1.f) cos_vis = cos_vis - 1e-6f;
-    }
-    out[0] = make_float4((float)axis[0], (float)axis[1], (float)axis[2], cos_occ);
-    out[1] = make_float4(cos_vis, sin_occ, sin_vis, 0.f);
+    cone_write(axis, mc, a0, a1, degen_s != 0, count, out);
   }
 }
 
@@ -463,19 +469,37 @@ int launch_prep_block_cones(const float4* pgeo, int64_t J, int block, int64_t nb
   return VISS_OK;
 }
 
-struct SnapMember {
-  int64_t base;
-  __device__ int operator()(int64_t i) const { return (int)(base + i); }
-};
-
-__global__ void snapshot_cones_kernel(const float4* satdir, int nsat, float4* cones) {
-  const int64_t s = blockIdx.x;
-  cone_block(satdir, nsat, SnapMember{s * nsat}, cones + 2 * s);
+// One thread per snapshot (its nsat satellites in a loop): the bounds of
+// cone_block, without a block's reductions and serial tail per snapshot.
+__global__ void snapshot_cones_kernel(const float4* satdir, int64_t S, int nsat, float4* cones) {
+  const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const float4* d0 = satdir + s * nsat;
+  bool degen = false;
+  double sx = 0, sy = 0, sz = 0;
+  for (int i = 0; i < nsat; ++i) {
+    const float4 d = d0[i];
+    if (d.x == 0.f && d.y == 0.f && d.z == 0.f) { degen = true; continue; }
+    if (d.w == 0.f) degen = true;  // inside the sphere: no cone
+    sx -= d.x; sy -= d.y; sz -= d.z;
+  }
+  const double nn = sqrt(sx * sx + sy * sy + sz * sz);
+  double axis[3] = {nn > 0 ? sx / nn : 0, nn > 0 ? sy / nn : 0, nn > 0 ? sz / nn : 1};
+  if (!(nn > 0)) degen = true;
+  double mc = 2.0, a0 = 10.0, a1 = -1.0;
+  for (int i = 0; i < nsat; ++i) {
+    const float4 d = d0[i];
+    mc = fmin(mc, -(axis[0] * d.x + axis[1] * d.y + axis[2] * d.z));
+    const double al = acos(fmin(1.0, fmax(-1.0, (double)d.w)));
+    a0 = fmin(a0, al);
+    a1 = fmax(a1, al);
+  }
+  cone_write(axis, mc, a0, a1, degen, nsat, cones + 2 * s);
 }
 
 int launch_prep_snapshot_cones(const float4* satdir, int64_t S, int nsat, float4* cones, cudaStream_t st) {
   if (S <= 0) return VISS_OK;
-  snapshot_cones_kernel<<<(unsigned)S, 32, 0, st>>>(satdir, nsat, cones);
+  snapshot_cones_kernel<<<(unsigned)((S + 127) / 128), 128, 0, st>>>(satdir, S, nsat, cones);
   VISS_LAUNCH_CHECK("snapshot_cones_kernel");
   return VISS_OK;
 }
