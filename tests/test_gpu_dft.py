@@ -257,13 +257,20 @@ def test_vis_recon_geometric(V, oracle, occ, prec):
     assert rms <= tol[0] and mx <= tol[1], ("recon", occ, prec, rms, mx)
 
 
-def test_geometric_mask_exact_counts(V, oracle):
+@pytest.mark.parametrize("order", ["snapshot", "shuffled"])
+def test_geometric_mask_exact_counts(V, oracle, order):
     """Zero phase, brightness 0, occluded value 1: V_k = number of occluded pixels of row k;
     recon of V = 1 gives K * F_j = number of rows that see pixel j.  Both exact integers,
     compared with the FP64 oracle mask; decisions within 1e-9 rad of a limb are counted
-    and excluded."""
+    and excluded.  In snapshot order a block of 1,024 visibilities uses ~300 satellites and
+    the vis kernel decides each (straddling pixel, satellite) once per tile; shuffled, a
+    block spans the whole orbit (~5,760 satellites), the vis kernel tests each term's two
+    satellites instead and the recon sees snapshot runs of one row."""
     pos, u, v, w, snap, pair = small_geometry(V)
     K = u.numel()
+    if order == "shuffled":
+        perm = torch.from_numpy(np.random.default_rng(11).permutation(K)).cuda()
+        u, v, w, snap, pair = (t[perm].contiguous() for t in (u, v, w, snap, pair))
     J = 4000
     l, m, n, _ = sky(J)
     z = torch.zeros(K, dtype=torch.float32, device="cuda")
