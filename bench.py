@@ -35,7 +35,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Gterms/s shaded vis-DFT + recon, 1 GB300, chosen vs plain at ≤1e-5 rel err"
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu
 # capture of this workload at full size (the command is kept with the ncu summaries).
-TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 199.85e6, "recon_fast_kernel": 299.11e6}}
+TRAFFIC_BYTES = {"cfg2_10MHz": {"vis_fast_kernel": 198.76e6, "recon_fast_kernel": 297.08e6}}
 UNIT = "Gterms/s"
 L2_FLUSH_BYTES = 256 << 20
 
