@@ -12,10 +12,13 @@
 // same as in the vis kernel: 3 IMAD [+3 FFMA fractional uvw] [+3 FFMA
 // compensated], turns -> angle, __sincosf, 2 FFMA with |y_k|.
 // Masks:
-//   GEOMETRIC: rows come in snapshot runs; per run every thread tests its pixels
-//     against the snapshot's bounding cone and the warp votes: all occluded ->
-//     the run is skipped, all visible -> unmasked loop, else the thread builds a
-//     per-pixel satellite occlusion bitmask and tests each row's pair.
+//   GEOMETRIC: rows hidden from the whole pixel block are dropped when a tile is
+//     loaded; the rest come in snapshot runs.  Per run the warp tests the cap
+//     bounding its 128 pixels against the snapshot's cones (warp-uniform); where
+//     that leaves the run open, every thread tests its pixels against the
+//     snapshot's bounding cone and the warp votes: all occluded -> the run is
+//     skipped, all visible -> unmasked loop, else the thread builds a per-pixel
+//     satellite occlusion bitmask and tests each row's pair.
 //   REF: the reference ratio mask can only fire on pixels (thetaP, phiP) with
 //     1 <= thetaP <= tmax_k, 1 <= phiP <= pmax_k; tiles whose rows cannot touch
 //     the item's pixels run unmasked.

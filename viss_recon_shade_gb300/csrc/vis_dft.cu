@@ -13,8 +13,11 @@
 //   GEOMETRIC: pixels are classified against a cone bounding the shadow cones
 //     of every satellite used by the CTA's rows -- all visible / all occluded /
 //     mixed -- and compacted into a fast list (brightness or occluded value,
-//     no per-term test) and a mixed list (per-term test against the row's two
-//     satellites, decided in double within GEO_EPS of the limb).
+//     no per-term test) and a mixed list.  Each (mixed pixel, satellite of the
+//     block's rows) pair is decided once per tile into shared-memory bits (in
+//     double within GEO_EPS of the limb); a term ORs its row's two satellite
+//     bits.  Blocks whose rows span too many satellites for the bits test the
+//     row's two satellites per term instead.
 //   REF_*: per-row window (row range x column range on the fine grid); tiles
 //     no window of the CTA touches run the unmasked loop.
 // Pixel chunks give partial sums, reduced in a fixed order.
