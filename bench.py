@@ -349,6 +349,36 @@ def run_ours(args, ws, rank, local):
         step()  # restore the chosen outputs
         torch.cuda.synchronize()
 
+    # ---- the reference programs' own mask on the same inputs ------------------
+    # REF_QUIRK windows (RES 20940, the shade10M grid) from viss_shade_windows on these
+    # uvw, the reference's phase convention and occluded value: the inputs the
+    # reference arm's ref_cuda_* legs give the reference's kernels
+    ref_mode = None
+    if not args.no_ref_cuda and ws == 1:
+        RES = 20940
+        raw, _ = V.shade_windows(d["u"], d["v"], d["w"], RES)
+        shade = V.normalise_shade(raw)
+        rcfg = V.DftConfig.reference(RES, precision=prec)
+        Vr, Fr = torch.empty_like(Vout), torch.empty_like(Fout)
+        r = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        for i in range(2):  # a warm-up pass, then the timed one
+            flush.zero_()
+            r[0].record(st)
+            V.vis_dft(rcfg, d["u"], d["v"], d["w"], d["l"], d["m"], d["n"], d["b"], shade=shade, out=Vr)
+            r[1].record(st)
+            V.recon(rcfg, d["u"], d["v"], d["w"], Vr, d["l"], d["m"], d["n"], shade=shade, out=Fr)
+            r[2].record(st)
+            torch.cuda.synchronize()
+        rms = r[0].elapsed_time(r[2])
+        ref_mode = {"value": round(terms_step / (rms * 1e-3) / 1e9, 3), "unit": UNIT,
+                    "vis_ms": round(r[0].elapsed_time(r[1]), 2), "recon_ms": round(r[1].elapsed_time(r[2]), 2),
+                    "precision": precision_name(d, args.precision),
+                    "what": "REF_QUIRK: the reference programs' window mask as written (vissGen10M_shade.cu:130), "
+                            "windows from viss_shade_windows at RES 20940 on these uvw (bit-exact with the "
+                            "reference's stage 2), its phase convention and occluded value 240: the inputs of "
+                            "the reference arm's ref_cuda_* legs"}
+        del Vr, Fr, shade, raw
+
     # ---- CPU baseline (oracle, bounded sample) + accuracy on the sample -------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
@@ -363,6 +393,8 @@ def run_ours(args, ws, rank, local):
                     "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
             "roofline": roofline, "gpu_launches": launches, "clocks": clk.summary(),
             "plain": plain, "cpu_baseline": cpu}
+    if ref_mode:
+        line["ref_mode"] = ref_mode
     if plain:
         line["speedup_vs_plain"] = round(value / plain["value"], 2)
     if not args.no_stage1:
