@@ -18,8 +18,8 @@
 //     double within GEO_EPS of the limb); a term ORs its row's two satellite
 //     bits.  Blocks whose rows span too many satellites for the bits test the
 //     row's two satellites per term instead.
-//   REF_*: per-row window (row range x column range on the fine grid); tiles
-//     no window of the CTA touches run the unmasked loop.
+//   REF_*: per-row window (row range x column range on the fine grid); a warp
+//     none of whose 128 windows reaches the tile runs the unmasked loop.
 // Pixel chunks give partial sums, reduced in a fixed order.
 #include "viss_internal.cuh"
 
@@ -294,7 +294,9 @@ __device__ __forceinline__ void vis_body(const VisParams& p, VisSmem<MASK, COMP,
           }
         }
       }
-      masked_tile = __syncthreads_or(hit) != 0;
+      // per warp: a warp none of whose 128 windows reaches the tile runs the unmasked loop
+      __syncthreads();  // the tile's records are in shared memory
+      masked_tile = __any_sync(0xffffffffu, hit);
     }
 
     if (!masked_tile) {
