@@ -61,11 +61,17 @@ def parse_args():
 
 
 # ------------------------------------------------------------------ distributed
-def dist_setup():
+def dist_setup(group: bool = True, cuda: bool = True):
+    """(world size, rank, local rank) from the launcher's environment; with `group`
+    a NCCL process group over the ranks (N > 1), with `cuda` this rank's GPU selected."""
     import torch
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not group:
+        if cuda:
+            torch.cuda.set_device(local)
+        return ws, rank, local
     if ws > 1:
         import torch.distributed as dist
         torch.cuda.set_device(local)
@@ -1068,11 +1074,16 @@ def main():
     if args.workload == "textio":
         run_textio(args)
         return
+    if args.impl == "reference":
+        # rank 0 alone runs the reference's CPU implementation (no collective); a GPU
+        # only for its ref_cuda_* legs
+        rank = int(os.environ.get("RANK", "0"))
+        ws, rank, local = dist_setup(group=False, cuda=rank == 0 and not args.no_ref_cuda)
+        run_reference(args, ws, rank, local)
+        return
     ws, rank, local = dist_setup()
     from viss_recon_shade_gb300.synth import BATCH_WORKLOADS
-    if args.impl == "reference":
-        run_reference(args, ws, rank, local)
-    elif args.workload in BATCH_WORKLOADS:
+    if args.workload in BATCH_WORKLOADS:
         run_batch(args, ws, rank, local)
     elif args.workload == "stage1":
         run_stage1(args, ws, rank, local)
