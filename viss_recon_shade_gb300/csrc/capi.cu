@@ -158,13 +158,14 @@ static void plan_vis(VisPlan& p, const viss_dft_cfg& cfg, const Batch& bt, int64
   p.nrb = bt.ch.rb_off[bt.ch.nch];
   p.Kpad = (p.nrb > 0 ? p.nrb : 1) * VIS_ROWS;
   p.nsd = (geo && p.geo) ? geo->S * (int64_t)geo->nsat : 0;
-  // Split the sky into chunks until there are ~32 work items (visibility block x
+  // Split the sky into chunks until there are ~64 work items (visibility block x
   // sky chunk) per resident CTA: blocks see different occluded fractions of the sky,
-  // and short items balance them (10 MHz vis: 1 chunk 158 ms, 2 149 ms, 16 143 ms).
+  // and short items balance them (10 MHz vis: 1 chunk 158 ms, 2 149 ms, 9 143.3 ms,
+  // 16 142.6 ms, 24 142.5 ms).
   const int64_t slots = planned_ctas(tn, VISS_VIS_MINB);
   int64_t nsplit = 1;
   if (tn.vis_split > 0) nsplit = tn.vis_split;
-  else if (p.nrb > 0 && p.nrb < 32 * slots) nsplit = (32 * slots + p.nrb - 1) / p.nrb;
+  else if (p.nrb > 0 && p.nrb < 64 * slots) nsplit = (64 * slots + p.nrb - 1) / p.nrb;
   const int64_t maxsplit = (J + VIS_P - 1) / VIS_P;
   if (nsplit > maxsplit) nsplit = maxsplit;
   if (nsplit < 1) nsplit = 1;
